@@ -1,0 +1,353 @@
+"""Benchmark of the differentiable SH Gaussian-splatting step on one GB300.
+
+Workload (default ``headline``): 1,000,000 Gaussians, SH degree 3, one
+1920x1080 view, 16x16 tiles, fp32; a step is one forward + backward of
+loss = sum(image * W) through the fused native path (projection, binning,
+raster forward, raster backward, projection backward), i.e. the gradients of
+all five parameter tensors.  Metric: fwd+bwd ms/iter (lower is better).
+
+Printed JSON line (rank 0): value = device-timed ms per step with the scene
+resident in HBM (CUDA events over K steps, max over ranks); ``e2e`` = the same
+step through the public API with pinned host buffers, host->device copy of the
+parameters and the loss weights and device->host copy of the image and all
+gradients inside the timed region; ``roofline`` for the dominant kernel from
+per-stage CUDA events inside the timed region; ``cpu_baseline`` = the CPU
+oracle on a bounded sample of the same workload.
+
+``--impl reference`` times the reference's path on the host CPU cores (the C
+restatement of its kernels in oracle/, all threads) on the same workload.
+With --gpus N > 1 every rank renders its own replica (views are independent);
+there is no collective.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return PEAKS_FALLBACK, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def algorithmic_bytes(stage, n, K, P, C, n_tiles, n_pairs_tg=None):
+    """Bytes a stage must move at minimum (per launch), as documented for the roofline."""
+    CC = C * C
+    if stage == "project":
+        return n * (44 + 52)
+    if stage == "binning":
+        # depth sort 4 passes (r+w key+value) + histogram, emission, tile sort 2 passes, ranges
+        return n * (4 * 16 + 4 + 4 + 20) + K * (8 + 2 * 16 + 4 + 4) + 8 * n_tiles
+    if stage == "raster_fwd":
+        return K * (32 + 12 * CC) + 12 * P
+    if stage == "raster_bwd":
+        return K * (32 + 12 * CC) + 36 * P + K * 4 * (6 + 3 * CC)
+    if stage == "project_bwd":
+        return n * (44 + 32 + 44)
+    return 0
+
+
+def run_gsx(args):
+    import torch
+
+    from gaussian_splatting_3d_gb300 import renderer, scene as S
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    wl = S.headline_workload(n=args.n) if args.workload == "headline" else S.small_workload()
+    sc, view = wl.scene, wl.views[0]
+    settings = renderer.RasterSettings(tile_w=view.tile, tile_h=view.tile)
+    params = [torch.from_numpy(a).to(dev) for a in (sc.mean, sc.qvec, sc.log_scale, sc.sh, sc.alpha_logit)]
+    W = torch.from_numpy(wl.grad_weight).to(dev)
+    pipe = renderer.ViewPipeline(dev)
+
+    def step(timer=None):
+        state = pipe.forward(*params, view.c2w, view.cam, settings, timer=timer)
+        grads = pipe.backward(state, *params, W, timer=timer)
+        return state, grads
+
+    for _ in range(args.warmup):
+        state, grads = step()
+    torch.cuda.synchronize()
+    K = state["K"]
+    visible = int((state["pr"].counts > 0).sum().item())
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    timer = renderer.StageTimer()
+    barrier()
+    clocks.start()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    wall0 = time.perf_counter()
+    t0.record()
+    for _ in range(args.steps):
+        step(timer)
+    t1.record()
+    barrier()
+    wall1 = time.perf_counter()
+    clock_info = clocks.stop()
+    ms = t0.elapsed_time(t1) / args.steps
+    if world > 1:
+        import torch.distributed as dist
+
+        tt = torch.tensor([ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    stages = timer.summary()
+
+    # end-to-end through the public autograd API with host buffers
+    host = [torch.from_numpy(a).pin_memory() for a in (sc.mean, sc.qvec, sc.log_scale, sc.sh, sc.alpha_logit)]
+    Wh = torch.from_numpy(wl.grad_weight).pin_memory()
+    out_host = [torch.empty(a.shape, dtype=torch.float32).pin_memory() for a in
+                (sc.mean, sc.qvec, sc.log_scale, sc.sh, sc.alpha_logit)]
+    img_host = torch.empty((view.cam.h, view.cam.w, 3), dtype=torch.float32).pin_memory()
+    loss_host = torch.empty((), dtype=torch.float32).pin_memory()
+
+    def e2e_step():
+        ps = [h.to(dev, non_blocking=True).requires_grad_(True) for h in host]
+        w = Wh.to(dev, non_blocking=True)
+        img = renderer.rasterize(*ps, view.c2w, view.cam, settings)
+        loss = (img * w).sum()
+        loss.backward()
+        for p, o in zip(ps, out_host):
+            o.copy_(p.grad, non_blocking=True)
+        img_host.copy_(img.detach(), non_blocking=True)
+        loss_host.copy_(loss.detach(), non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record()
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    h2d = sum(h.numel() * 4 for h in host) + Wh.numel() * 4
+    d2h = sum(o.numel() * 4 for o in out_host) + img_host.numel() * 4 + 4
+
+    if rank != 0:
+        return
+    peaks, peaks_kind = load_peaks()
+    P = view.cam.w * view.cam.h
+    n_tiles = settings.tiles(view.cam)[0] * settings.tiles(view.cam)[1]
+    dom = max(stages, key=lambda k: stages[k]["mean_ms"])
+    alg = algorithmic_bytes(dom, sc.n, K, P, sc.sh_order, n_tiles)
+    achieved = alg / (stages[dom]["mean_ms"] * 1e-3) / 1e9
+    peak = float(peaks["hbm_gbs"])
+    line = {
+        "metric": "fwd+bwd ms/iter (1M Gaussians, 1920x1080)",
+        "value": round(ms, 4),
+        "unit": "ms/iter",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms, 4),
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded PCG64 scene of the headline shape; no dataset)",
+        "config": {"workload": f"{args.workload}: {sc.n} Gaussians, SH degree {sc.sh_order - 1}, "
+                               f"{view.cam.w}x{view.cam.h}, tile {view.tile}x{view.tile}, fwd+bwd",
+                   "n_gaussians": sc.n, "visible": visible, "keys": K, "width": view.cam.w,
+                   "height": view.cam.h, "sh_degree": sc.sh_order - 1, "tile": view.tile,
+                   "l2": "inputs larger than L2 (scene parameters %.0f MB)" % (
+                       sum(p.numel() * 4 for p in params) / 1e6),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "stages_ms": {k: round(v["mean_ms"], 4) for k, v in stages.items()},
+        "e2e": {"value": round(e2e_ms, 4), "unit": "ms/iter", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 2), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "peak_source": f"{peaks_kind} hbm_gbs", "algorithmic_bytes": int(alg)},
+        "clocks": clock_info,
+        "gpu_launches": None,
+        "wall_s": round(wall1 - wall0, 3),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(wl, args.cpu_frac)
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(wl, frac: float):
+    """The CPU oracle (C restatement of the reference's kernels, OpenMP over
+    tiles) on a bounded sample: projection and binning on the whole scene,
+    raster forward + backward on every k-th tile row, scaled to the frame."""
+    from oracle import oracle as O
+    from gaussian_splatting_3d_gb300.camera import frustum_np
+
+    sc, view = wl.scene, wl.views[0]
+    cam = view.cam
+    t0 = time.perf_counter()
+    normals, pts = frustum_np(view.c2w, cam)
+    ocam = O.make_camera(view.c2w, cam.fx, cam.fy, cam.cx, cam.cy, cam.w, cam.h, normals, pts)
+    pr = O.project(sc.mean, sc.qvec, sc.log_scale, sc.alpha_logit, ocam, 1.0, 6.0, view.tile, view.tile)
+    ntw, nth = (cam.w + view.tile - 1) // view.tile, (cam.h + view.tile - 1) // view.tile
+    b = O.bin_gaussians(pr["rect"], pr["rect"][:, 2:], pr["depth"], nth, ntw, stride=4)
+    t1 = time.perf_counter()
+    every = max(1, int(round(1.0 / frac)))
+    rows = np.arange(nth) % every == 0
+    start = b["start"].reshape(nth, ntw).copy()
+    end = b["end"].reshape(nth, ntw).copy()
+    start[~rows] = -1
+    end[~rows] = -1
+    P = O.raster_params(cam.w, cam.h, view.tile, view.tile, sc.sh_order, sc.sh.shape[-1])
+    tl = np.array(cam.topleft(), np.float32)
+    psx, psy = np.float32(1 / cam.fx), np.float32(1 / cam.fy)
+    t2 = time.perf_counter()
+    img = O.render_fwd(P, pr["mean2d"], pr["cov2d"], sc.sh, pr["alpha"], start.reshape(-1), end.reshape(-1),
+                       b["ids"], tl, view.c2w, psx, psy)
+    g = O.render_bwd(P, pr["mean2d"], pr["cov2d"], sc.sh, pr["alpha"], start.reshape(-1), end.reshape(-1),
+                     b["ids"], tl, view.c2w, psx, psy, img, wl.grad_weight)
+    O.project_bwd(sc.mean, sc.qvec, sc.log_scale, sc.alpha_logit, ocam, pr["mask"], g["mean2d"], g["cov2d"],
+                  g["alpha"])
+    t3 = time.perf_counter()
+    sampled = float(rows.sum()) / nth
+    total_s = (t1 - t0) + (t3 - t2) / sampled
+    return {"value": round(total_s * 1e3, 1), "unit": "ms/iter", "cores": O.num_threads(), "kind": "port",
+            "sample": f"projection + binning on all {sc.n} Gaussians; raster fwd+bwd on every {every}-th tile row "
+                      f"({int(rows.sum())}/{nth} rows), time scaled by {1 / sampled:.2f}"}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    from gaussian_splatting_3d_gb300 import scene as S
+
+    wl = S.headline_workload(n=args.n) if args.workload == "headline" else S.small_workload()
+    for _ in range(args.warmup):
+        cpu_baseline(wl, args.cpu_frac)
+    vals = [cpu_baseline(wl, args.cpu_frac) for _ in range(args.steps)]
+    v = float(np.mean([x["value"] for x in vals]))
+    sc, view = wl.scene, wl.views[0]
+    line = {
+        "impl": "reference",
+        "metric": "fwd+bwd ms/iter (1M Gaussians, 1920x1080)",
+        "value": round(v, 1),
+        "unit": "ms/iter",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(v, 1),
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded PCG64 scene of the headline shape; no dataset)",
+        "config": {"workload": f"{args.workload}: {sc.n} Gaussians, SH degree {sc.sh_order - 1}, "
+                               f"{view.cam.w}x{view.cam.h}, tile {view.tile}x{view.tile}, fwd+bwd"},
+        "cpu_baseline": dict(vals[-1], value=round(v, 1)),
+        "e2e": {"value": round(v, 1), "unit": "ms/iter", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gsx", choices=["gsx", "reference"])
+    ap.add_argument("--workload", default="headline", choices=["headline", "small"])
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-frac", type=float, default=1.0 / 8.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gsx(args)
+
+
+if __name__ == "__main__":
+    main()

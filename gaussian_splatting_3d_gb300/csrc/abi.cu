@@ -1,0 +1,347 @@
+// abi.cu -- the extern "C" entry points declared in include/gsx.h: argument
+// validation, status codes and a per-thread error message.  No entry point
+// exits the process or allocates device memory.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+
+#include "gsx_internal.cuh"
+
+namespace gsx {
+
+namespace {
+thread_local char g_err[512] = {0};
+}
+
+void set_error(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+int cuda_status(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return GSX_OK;
+  set_error("%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+  return GSX_ERR_CUDA;
+}
+
+}  // namespace gsx
+
+using namespace gsx;
+
+#define GSX_REQUIRE(cond, ...)      \
+  do {                              \
+    if (!(cond)) {                  \
+      set_error(__VA_ARGS__);       \
+      return GSX_ERR_INVALID_ARG;   \
+    }                               \
+  } while (0)
+
+static inline cudaStream_t as_stream(void *s) { return static_cast<cudaStream_t>(s); }
+
+extern "C" {
+
+const char *gsx_status_string(int status) {
+  switch (status) {
+    case GSX_OK: return "ok";
+    case GSX_ERR_INVALID_ARG: return "invalid argument";
+    case GSX_ERR_CAPACITY: return "capacity exceeded";
+    case GSX_ERR_TIMEOUT: return "device wait timed out";
+    case GSX_ERR_CUDA: return "CUDA error";
+    case GSX_ERR_MISMATCH: return "size mismatch";
+  }
+  return "unknown status";
+}
+
+const char *gsx_last_error(void) { return g_err; }
+
+int gsx_abi_version(void) { return 1; }
+
+int gsx_culling_gaussian_bsphere(int64_t n, const float *mean, const float *qvec,
+                                 const float *svec, const float *normal,
+                                 const float *pts, uint8_t *mask, float thresh,
+                                 void *stream) {
+  (void)qvec;
+  g_err[0] = 0;
+  GSX_REQUIRE(n >= 0, "n must be >= 0 (got %lld)", (long long)n);
+  if (n == 0) return GSX_OK;
+  GSX_REQUIRE(mean && svec && normal && pts && mask, "null pointer argument");
+  return launch_cull_bsphere(n, mean, svec, normal, pts, mask, thresh, as_stream(stream));
+}
+
+size_t gsx_binning_workspace_bytes(int64_t n_gaussians, int64_t key_capacity,
+                                   int64_t n_tiles) {
+  if (n_gaussians < 0 || key_capacity < 0 || n_tiles < 0) return 0;
+  return binning_workspace_bytes(n_gaussians, key_capacity, n_tiles);
+}
+
+static int check_binning_sizes(int64_t n, int64_t cap, int32_t nth, int32_t ntw) {
+  GSX_REQUIRE(n >= 0 && n < (1ll << 30), "n must be in [0, 2^30) (got %lld)", (long long)n);
+  GSX_REQUIRE(cap >= 0 && cap < (1ll << 30), "key count must be in [0, 2^30) (got %lld)",
+              (long long)cap);
+  GSX_REQUIRE(nth > 0 && ntw > 0, "tile grid must be positive (got %d x %d)", ntw, nth);
+  GSX_REQUIRE((int64_t)nth * ntw < (1ll << 31), "too many tiles");
+  return GSX_OK;
+}
+
+int gsx_tile_culling_aabb_start_end(int64_t n, int64_t n_keys,
+                                    const int32_t *aabb_topleft,
+                                    const int32_t *aabb_bottomright,
+                                    const float *depth, int32_t n_tiles_h,
+                                    int32_t n_tiles_w, int32_t *gaussian_ids,
+                                    int32_t *start, int32_t *end, void *workspace,
+                                    size_t workspace_bytes, void *stream) {
+  g_err[0] = 0;
+  int st = check_binning_sizes(n, n_keys, n_tiles_h, n_tiles_w);
+  if (st != GSX_OK) return st;
+  GSX_REQUIRE(start && end, "null start/end");
+  GSX_REQUIRE(n == 0 || (aabb_topleft && aabb_bottomright && depth), "null input pointer");
+  GSX_REQUIRE(n_keys == 0 || gaussian_ids, "null gaussian_ids");
+  GSX_REQUIRE(workspace || workspace_bytes == 0, "null workspace");
+  int64_t got = 0;
+  st = run_binning(n, aabb_topleft, aabb_bottomright, 2, nullptr, depth, n_tiles_w, n_tiles_h,
+                   n_keys, gaussian_ids, start, end, &got, workspace, workspace_bytes,
+                   as_stream(stream));
+  if (st == GSX_ERR_CAPACITY && got != n_keys) st = GSX_OK;  // reported below
+  if (st != GSX_OK) return st;
+  if (got != n_keys) {
+    set_error("the rectangles hold %lld keys but gaussian_ids has %lld entries",
+              (long long)got, (long long)n_keys);
+    return GSX_ERR_MISMATCH;
+  }
+  return GSX_OK;
+}
+
+int gsx_bin_gaussians(int64_t n, const int32_t *rect, const int32_t *counts,
+                      const float *depth, int32_t n_tiles_w, int32_t n_tiles_h,
+                      int64_t key_capacity, int32_t *gaussian_ids, int32_t *start,
+                      int32_t *end, int64_t *n_keys_out, void *workspace,
+                      size_t workspace_bytes, void *stream) {
+  g_err[0] = 0;
+  int st = check_binning_sizes(n, key_capacity, n_tiles_h, n_tiles_w);
+  if (st != GSX_OK) return st;
+  GSX_REQUIRE(start && end && n_keys_out, "null output pointer");
+  GSX_REQUIRE(n == 0 || (rect && counts && depth), "null input pointer");
+  GSX_REQUIRE(key_capacity == 0 || gaussian_ids, "null gaussian_ids");
+  return run_binning(n, rect, rect + 2, 4, counts, depth, n_tiles_w, n_tiles_h, key_capacity,
+                     gaussian_ids, start, end, n_keys_out, workspace, workspace_bytes,
+                     as_stream(stream));
+}
+
+static int check_raster(const RasterArgs &a, int C, int64_t n, int64_t n_keys) {
+  GSX_REQUIRE(C >= 1 && C <= 4, "SH order C must be 1..4 (got %d)", C);
+  GSX_REQUIRE(a.tile_w > 0 && a.tile_h > 0 && a.tile_w * a.tile_h <= 1024,
+              "tile must have 1..1024 pixels (got %d x %d)", a.tile_w, a.tile_h);
+  GSX_REQUIRE(a.width > 0 && a.height > 0, "image size must be positive");
+  GSX_REQUIRE((int64_t)a.n_tiles_w * a.tile_w >= a.width &&
+                  (int64_t)a.n_tiles_h * a.tile_h >= a.height,
+              "tile grid %d x %d of %d x %d tiles does not cover %d x %d", a.n_tiles_w,
+              a.n_tiles_h, a.tile_w, a.tile_h, a.width, a.height);
+  GSX_REQUIRE(a.sh_stride >= C * C, "sh_stride %d < C*C", a.sh_stride);
+  GSX_REQUIRE(n >= 0 && n_keys >= 0, "negative size");
+  GSX_REQUIRE(a.start && a.end && a.topleft && a.c2w && a.out, "null pointer argument");
+  GSX_REQUIRE(n_keys == 0 || a.ids, "null gaussian_ids");
+  GSX_REQUIRE(n == 0 || (a.mean2d && a.cov2d && a.sh && a.alpha), "null Gaussian data");
+  return GSX_OK;
+}
+
+static RasterArgs make_args(int64_t tile_w, int64_t tile_h, uint32_t ntw, uint32_t nth,
+                            float psx, float psy, uint32_t H, uint32_t W, float thresh) {
+  RasterArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.width = (int32_t)W;
+  a.height = (int32_t)H;
+  a.tile_w = (int32_t)tile_w;
+  a.tile_h = (int32_t)tile_h;
+  a.n_tiles_w = (int32_t)ntw;
+  a.n_tiles_h = (int32_t)nth;
+  a.psx = psx;
+  a.psy = psy;
+  a.T_thresh = thresh;
+  return a;
+}
+
+int gsx_tile_based_vol_rendering_sh(
+    int64_t n, int64_t n_keys, const float *mean, const float *cov,
+    const float *sh_coeffs, const float *alpha, const int32_t *start,
+    const int32_t *end, const int32_t *gaussian_ids, float *out,
+    const float *topleft, const float *c2w, uint32_t tile_size,
+    uint32_t n_tiles_h, uint32_t n_tiles_w, float pixel_size_x,
+    float pixel_size_y, uint32_t H, uint32_t W, uint32_t C, float thresh,
+    void *stream) {
+  g_err[0] = 0;
+  RasterArgs a = make_args(tile_size, tile_size, n_tiles_w, n_tiles_h, pixel_size_x,
+                           pixel_size_y, H, W, thresh);
+  a.sh_stride = (int32_t)(C * C);
+  a.mean2d = mean;
+  a.cov2d = cov;
+  a.sh = sh_coeffs;
+  a.alpha = alpha;
+  a.start = start;
+  a.end = end;
+  a.ids = gaussian_ids;
+  a.topleft = topleft;
+  a.c2w = c2w;
+  a.out = out;
+  a.write_empty = 0;
+  a.n = n;
+  a.n_keys = n_keys;
+  int st = check_raster(a, (int)C, n, n_keys);
+  if (st != GSX_OK) return st;
+  return launch_raster_forward(a, (int)C, as_stream(stream));
+}
+
+int gsx_tile_based_vol_rendering_backward_sh(
+    int64_t n, int64_t n_keys, const float *mean, const float *cov,
+    const float *sh_coeffs, const float *alpha, const int32_t *start,
+    const int32_t *end, const int32_t *gaussian_ids, const float *out,
+    float *grad_mean, float *grad_cov, float *grad_sh_coeffs, float *grad_alpha,
+    const float *grad_out, const float *topleft, const float *c2w,
+    uint32_t tile_size, uint32_t n_tiles_h, uint32_t n_tiles_w,
+    float pixel_size_x, float pixel_size_y, uint32_t H, uint32_t W, uint32_t C,
+    float thresh, void *stream) {
+  g_err[0] = 0;
+  RasterArgs a = make_args(tile_size, tile_size, n_tiles_w, n_tiles_h, pixel_size_x,
+                           pixel_size_y, H, W, thresh);
+  a.sh_stride = (int32_t)(C * C);
+  a.mean2d = mean;
+  a.cov2d = cov;
+  a.sh = sh_coeffs;
+  a.alpha = alpha;
+  a.start = start;
+  a.end = end;
+  a.ids = gaussian_ids;
+  a.topleft = topleft;
+  a.c2w = c2w;
+  a.out = const_cast<float *>(out);
+  a.final_img = out;
+  a.grad_out = grad_out;
+  a.g_mean2d = grad_mean;
+  a.g_cov2d = grad_cov;
+  a.g_sh = grad_sh_coeffs;
+  a.g_alpha = grad_alpha;
+  a.n = n;
+  a.n_keys = n_keys;
+  int st = check_raster(a, (int)C, n, n_keys);
+  if (st != GSX_OK) return st;
+  GSX_REQUIRE(grad_out && (n == 0 || (grad_mean && grad_cov && grad_sh_coeffs && grad_alpha)),
+              "null gradient pointer");
+  return launch_raster_backward(a, (int)C, as_stream(stream));
+}
+
+int gsx_project_forward(int64_t n, const float *mean, const float *qvec,
+                        const float *log_scale, const float *alpha_logit,
+                        const gsx_camera *cam, float frustum_radius,
+                        float tile_radius, int32_t tile_w, int32_t tile_h,
+                        int32_t scales_are_activated, float *mean2d, float *cov2d,
+                        float *depth, float *alpha, int32_t *rect,
+                        int32_t *counts, void *stream) {
+  g_err[0] = 0;
+  GSX_REQUIRE(n >= 0, "n must be >= 0");
+  GSX_REQUIRE(cam, "null camera");
+  GSX_REQUIRE(tile_w > 0 && tile_h > 0, "tile size must be positive");
+  GSX_REQUIRE(cam->width > 0 && cam->height > 0, "image size must be positive");
+  if (n == 0) return GSX_OK;
+  GSX_REQUIRE(mean && qvec && log_scale && mean2d && cov2d && depth && alpha && rect && counts,
+              "null pointer argument");
+  GSX_REQUIRE(((uintptr_t)qvec & 15) == 0 && ((uintptr_t)cov2d & 15) == 0 &&
+                  ((uintptr_t)rect & 15) == 0 && ((uintptr_t)mean2d & 7) == 0,
+              "qvec, cov2d and rect must be 16-byte aligned, mean2d 8-byte aligned");
+  return launch_project_forward(n, mean, qvec, log_scale, alpha_logit, *cam, frustum_radius,
+                                tile_radius, tile_w, tile_h, scales_are_activated, mean2d,
+                                cov2d, depth, alpha, rect, counts, as_stream(stream));
+}
+
+int gsx_render_forward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
+                       const float *mean2d, const float *cov2d, const float *sh,
+                       const float *alpha, const int32_t *start, const int32_t *end,
+                       const int32_t *gaussian_ids, const float *topleft,
+                       const float *c2w, float *out, void *stream) {
+  g_err[0] = 0;
+  GSX_REQUIRE(p, "null params");
+  RasterArgs a = make_args(p->tile_w, p->tile_h, (uint32_t)p->n_tiles_w,
+                           (uint32_t)p->n_tiles_h, p->pixel_size_x, p->pixel_size_y,
+                           (uint32_t)p->height, (uint32_t)p->width, p->T_thresh);
+  a.sh_stride = p->sh_stride;
+  a.mean2d = mean2d;
+  a.cov2d = cov2d;
+  a.sh = sh;
+  a.alpha = alpha;
+  a.start = start;
+  a.end = end;
+  a.ids = gaussian_ids;
+  a.topleft = topleft;
+  a.c2w = c2w;
+  a.out = out;
+  a.write_empty = p->write_empty_tiles;
+  a.n = n;
+  a.n_keys = n_keys;
+  int st = check_raster(a, p->sh_order, n, n_keys);
+  if (st != GSX_OK) return st;
+  return launch_raster_forward(a, p->sh_order, as_stream(stream));
+}
+
+int gsx_render_backward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
+                        const float *mean2d, const float *cov2d, const float *sh,
+                        const float *alpha, const int32_t *start,
+                        const int32_t *end, const int32_t *gaussian_ids,
+                        const float *topleft, const float *c2w, const float *out,
+                        const float *grad_out, float *grad_mean2d,
+                        float *grad_cov2d, float *grad_sh, float *grad_alpha,
+                        void *stream) {
+  g_err[0] = 0;
+  GSX_REQUIRE(p, "null params");
+  RasterArgs a = make_args(p->tile_w, p->tile_h, (uint32_t)p->n_tiles_w,
+                           (uint32_t)p->n_tiles_h, p->pixel_size_x, p->pixel_size_y,
+                           (uint32_t)p->height, (uint32_t)p->width, p->T_thresh);
+  a.sh_stride = p->sh_stride;
+  a.mean2d = mean2d;
+  a.cov2d = cov2d;
+  a.sh = sh;
+  a.alpha = alpha;
+  a.start = start;
+  a.end = end;
+  a.ids = gaussian_ids;
+  a.topleft = topleft;
+  a.c2w = c2w;
+  a.out = const_cast<float *>(out);
+  a.final_img = out;
+  a.grad_out = grad_out;
+  a.g_mean2d = grad_mean2d;
+  a.g_cov2d = grad_cov2d;
+  a.g_sh = grad_sh;
+  a.g_alpha = grad_alpha;
+  a.n = n;
+  a.n_keys = n_keys;
+  int st = check_raster(a, p->sh_order, n, n_keys);
+  if (st != GSX_OK) return st;
+  GSX_REQUIRE(grad_out && (n == 0 || (grad_mean2d && grad_cov2d && grad_sh && grad_alpha)),
+              "null gradient pointer");
+  return launch_raster_backward(a, p->sh_order, as_stream(stream));
+}
+
+int gsx_project_backward(int64_t n, const float *mean, const float *qvec,
+                         const float *log_scale, const float *alpha_logit,
+                         const gsx_camera *cam, const int32_t *counts,
+                         const float *grad_mean2d, const float *grad_cov2d,
+                         const float *grad_alpha, float *grad_mean,
+                         float *grad_qvec, float *grad_log_scale,
+                         float *grad_alpha_logit, void *stream) {
+  g_err[0] = 0;
+  GSX_REQUIRE(n >= 0, "n must be >= 0");
+  GSX_REQUIRE(cam, "null camera");
+  if (n == 0) return GSX_OK;
+  GSX_REQUIRE(mean && qvec && log_scale && alpha_logit && counts && grad_mean2d &&
+                  grad_cov2d && grad_alpha && grad_mean && grad_qvec && grad_log_scale &&
+                  grad_alpha_logit,
+              "null pointer argument");
+  GSX_REQUIRE(((uintptr_t)qvec & 15) == 0 && ((uintptr_t)grad_qvec & 15) == 0 &&
+                  ((uintptr_t)grad_cov2d & 15) == 0 && ((uintptr_t)grad_mean2d & 7) == 0,
+              "qvec, grad_qvec, grad_cov2d must be 16-byte aligned, grad_mean2d 8-byte");
+  return launch_project_backward(n, mean, qvec, log_scale, alpha_logit, *cam, counts,
+                                 grad_mean2d, grad_cov2d, grad_alpha, grad_mean, grad_qvec,
+                                 grad_log_scale, grad_alpha_logit, as_stream(stream));
+}
+
+}  // extern "C"

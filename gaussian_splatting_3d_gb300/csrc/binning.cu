@@ -1,0 +1,521 @@
+// binning.cu -- deterministic tile binning with a hand-written onesweep LSD
+// radix sort.
+//
+// The reference (gs/src/include/aabb_culling.h:15-41, 192-260) emits one
+// 64-bit key (tile_id << 32 | float bits of depth) per (Gaussian, tile of its
+// AABB) through a global atomic counter, sorts all 64 bits with CUB, and
+// derives start/end from the sorted tile ids (:70-103).  The same ordering is
+// produced here with far less K-sized traffic:
+//   1. sort the n Gaussians by depth bits (4 passes over n, not K, items);
+//   2. exclusive scan of their key counts in that order (decoupled look-back)
+//      and emission of (tile, Gaussian) pairs -- deterministic, no atomics;
+//   3. stable sort of the K pairs by tile id: ceil(log2(tiles)/8) passes;
+//   4. start/end from the tile boundaries.
+// Equal (tile, depth) keys come out in Gaussian-index order, i.e. the
+// reference's order after its non-deterministic ties are canonicalised.
+//
+// Onesweep pass (one launch per 8-bit digit): each CTA claims the next chunk
+// of 4096 keys through an atomic ticket (so every chunk it waits on belongs
+// to a CTA that is already running), ranks its keys stably per digit with
+// warp match + per-warp counters, publishes its digit counts, looks back over
+// the preceding chunks' counts for its global offsets, and scatters through
+// shared memory so that the global writes are runs of consecutive addresses.
+// Every wait on a predecessor is bounded; on expiry an error word is set and
+// the host returns GSX_ERR_TIMEOUT.
+#include "gsx_internal.cuh"
+
+namespace gsx {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kItems = 16;
+constexpr int kTile = kThreads * kItems;  // keys per chunk
+constexpr uint32_t kFlagAgg = 1u << 30;
+constexpr uint32_t kFlagPrefix = 2u << 30;
+constexpr uint32_t kCountMask = (1u << 30) - 1u;
+constexpr uint32_t kSpinLimit = 1u << 22;
+constexpr int kEmitItems = 8;
+constexpr int kEmitTile = kThreads * kEmitItems;
+constexpr unsigned long long kFlag64Agg = 1ull << 62;
+constexpr unsigned long long kFlag64Prefix = 2ull << 62;
+constexpr unsigned long long kCount64Mask = (1ull << 62) - 1ull;
+
+// error word bits
+constexpr uint32_t kErrTimeout = 1u;
+constexpr uint32_t kErrCount = 2u;
+constexpr uint32_t kErrRange = 4u;  // rectangle outside the tile grid
+constexpr uint32_t kErrIndex = 8u;  // corrupted depth order (after a timeout)
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+__device__ __forceinline__ uint32_t ld_volatile(const uint32_t *p) {
+  return *reinterpret_cast<const volatile uint32_t *>(p);
+}
+__device__ __forceinline__ void st_volatile(uint32_t *p, uint32_t v) {
+  *reinterpret_cast<volatile uint32_t *>(p) = v;
+}
+__device__ __forceinline__ unsigned long long ld_volatile64(const unsigned long long *p) {
+  return *reinterpret_cast<const volatile unsigned long long *>(p);
+}
+__device__ __forceinline__ void st_volatile64(unsigned long long *p, unsigned long long v) {
+  *reinterpret_cast<volatile unsigned long long *>(p) = v;
+}
+
+// Exclusive scan of one value per thread over a 256-thread block.
+template <typename T>
+__device__ __forceinline__ T block_exclusive_scan(T v, T *s_tmp, T *total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  T x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_tmp[w] = x;
+  __syncthreads();
+  T wsum = 0, all = 0;
+#pragma unroll
+  for (int k = 0; k < kWarps; ++k) {
+    T c = s_tmp[k];
+    if (k < w) wsum += c;
+    all += c;
+  }
+  __syncthreads();
+  if (total) *total = all;
+  return x - v + wsum;
+}
+
+// Histogram of `passes` 8-bit digits (starting at bit 0) of n keys.
+__global__ void __launch_bounds__(kThreads)
+    histogram_kernel(const uint32_t *__restrict__ keys, uint32_t n, int passes,
+                     uint32_t *__restrict__ hist) {
+  __shared__ uint32_t sh[4 * 256];
+  for (int i = threadIdx.x; i < 4 * 256; i += kThreads) sh[i] = 0;
+  __syncthreads();
+  for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const uint32_t k = keys[i];
+    for (int p = 0; p < passes; ++p) atomicAdd(&sh[p * 256 + ((k >> (8 * p)) & 255u)], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < passes * 256; i += kThreads)
+    if (sh[i]) atomicAdd(&hist[i], sh[i]);
+}
+
+// One stable LSD pass on the 8-bit digit at `shift`.  vals_in == nullptr
+// means value = input position.
+__global__ void __launch_bounds__(kThreads)
+    onesweep_kernel(const uint32_t *__restrict__ keys_in,
+                    const uint32_t *__restrict__ vals_in, uint32_t *__restrict__ keys_out,
+                    uint32_t *__restrict__ vals_out, uint32_t n, int shift,
+                    const uint32_t *__restrict__ pass_hist, uint32_t *status,
+                    uint32_t *chunk_counter, uint32_t *error) {
+  __shared__ uint32_t s_warp[kWarps][256];
+  __shared__ uint32_t s_cta_excl[256];
+  __shared__ uint32_t s_glob[256];
+  __shared__ uint32_t s_tmp[kWarps];
+  __shared__ uint32_t s_keys[kTile];
+  __shared__ uint32_t s_vals[kTile];
+  __shared__ uint32_t s_chunk;
+
+  const int t = threadIdx.x, w = t >> 5, lane = t & 31;
+  if (t == 0) s_chunk = atomicAdd(chunk_counter, 1u);
+  for (int i = t; i < kWarps * 256; i += kThreads) (&s_warp[0][0])[i] = 0;
+  __syncthreads();
+  const uint32_t chunk = s_chunk;
+  const uint32_t base = chunk * (uint32_t)kTile;
+  const uint32_t lt = lanemask_lt();
+
+  uint32_t keys[kItems], vals[kItems], rank[kItems];
+#pragma unroll
+  for (int j = 0; j < kItems; ++j) {
+    const uint32_t idx = base + w * (32 * kItems) + j * 32 + lane;
+    const bool valid = idx < n;
+    const uint32_t k = valid ? keys_in[idx] : 0u;
+    keys[j] = k;
+    vals[j] = valid ? (vals_in ? vals_in[idx] : idx) : 0u;
+    const uint32_t d = (k >> shift) & 255u;
+    const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 256u);
+    uint32_t cnt = 0;
+    if (valid) cnt = s_warp[w][d];
+    __syncwarp();
+    const uint32_t r = __popc(peers & lt);
+    if (valid && r == 0) s_warp[w][d] = cnt + __popc(peers);
+    rank[j] = cnt + r;
+    __syncwarp();
+  }
+  __syncthreads();
+
+  // per digit (thread t = digit t): exclusive prefix over warps, CTA total
+  uint32_t total = 0;
+#pragma unroll
+  for (int ww = 0; ww < kWarps; ++ww) {
+    const uint32_t c = s_warp[ww][t];
+    s_warp[ww][t] = total;
+    total += c;
+  }
+  const uint32_t cta_excl = block_exclusive_scan<uint32_t>(total, s_tmp, nullptr);
+  s_cta_excl[t] = cta_excl;
+  const uint32_t gbase = block_exclusive_scan<uint32_t>(pass_hist[t], s_tmp, nullptr);
+
+  // decoupled look-back for digit t
+  uint32_t prev = 0;
+  uint32_t *mine = status + (size_t)chunk * 256 + t;
+  if (chunk == 0) {
+    st_volatile(mine, kFlagPrefix | total);
+  } else {
+    st_volatile(mine, kFlagAgg | total);
+    int64_t c = (int64_t)chunk - 1;
+    uint32_t spins = 0;
+    while (c >= 0) {
+      const uint32_t sv = ld_volatile(status + (size_t)c * 256 + t);
+      const uint32_t flag = sv & ~kCountMask;
+      if (flag == 0u) {
+        if (++spins > kSpinLimit) {
+          atomicOr(error, kErrTimeout);
+          break;
+        }
+        __nanosleep(32);
+        continue;
+      }
+      prev += sv & kCountMask;
+      if (flag == kFlagPrefix) break;
+      --c;
+    }
+    st_volatile(mine, kFlagPrefix | (prev + total));
+  }
+  s_glob[t] = gbase + prev;
+  __syncthreads();
+
+#pragma unroll
+  for (int j = 0; j < kItems; ++j) {
+    const uint32_t idx = base + w * (32 * kItems) + j * 32 + lane;
+    if (idx < n) {
+      const uint32_t d = (keys[j] >> shift) & 255u;
+      const uint32_t pos = s_cta_excl[d] + s_warp[w][d] + rank[j];
+      s_keys[pos] = keys[j];
+      s_vals[pos] = vals[j];
+    }
+  }
+  __syncthreads();
+  const uint32_t cnt = min((uint32_t)kTile, n - base);
+  for (uint32_t i = t; i < cnt; i += kThreads) {
+    const uint32_t k = s_keys[i];
+    const uint32_t d = (k >> shift) & 255u;
+    const uint32_t gpos = s_glob[d] + (i - s_cta_excl[d]);
+    if (gpos < n) {  // always true unless a look-back wait expired
+      keys_out[gpos] = k;
+      vals_out[gpos] = s_vals[i];
+    }
+  }
+}
+
+// Keys of one rectangle, capped at 2^31 (far above any key capacity) so the
+// 62-bit scan cannot overflow for up to 2^30 Gaussians.
+__device__ __forceinline__ long long rect_count(const int32_t *tl, const int32_t *br) {
+  const long long w = (long long)br[0] - tl[0] + 1, h = (long long)br[1] - tl[1] + 1;
+  if (w <= 0 || h <= 0) return 0;
+  if (w >= (1ll << 31) || h >= (1ll << 31)) return 1ll << 31;
+  const long long c = w * h;
+  return c < (1ll << 31) ? c : (1ll << 31);
+}
+
+// Exclusive scan of key counts in depth order (decoupled look-back over
+// chunks of 2048 Gaussians) fused with the emission of (tile, Gaussian)
+// pairs.  The last chunk writes the key total.
+__global__ void __launch_bounds__(kThreads)
+    emit_kernel(const uint32_t *__restrict__ order, uint32_t n,
+                const int32_t *__restrict__ rect_tl, const int32_t *__restrict__ rect_br,
+                int rect_stride, const int32_t *__restrict__ counts, int32_t n_tiles_w,
+                int32_t n_tiles_h, uint32_t *__restrict__ tile_out, uint32_t *__restrict__ id_out,
+                unsigned long long capacity, unsigned long long *status,
+                uint32_t *chunk_counter, unsigned long long *total_out, uint32_t *error) {
+  __shared__ unsigned long long s_tmp[kWarps];
+  __shared__ unsigned long long s_prefix;
+  __shared__ uint32_t s_chunk;
+  const int t = threadIdx.x;
+  if (t == 0) s_chunk = atomicAdd(chunk_counter, 1u);
+  __syncthreads();
+  const uint32_t chunk = s_chunk;
+  const uint32_t first = chunk * (uint32_t)kEmitTile + t * kEmitItems;
+  uint32_t gid[kEmitItems];
+  long long cnt[kEmitItems];
+  unsigned long long mysum = 0;
+#pragma unroll
+  for (int j = 0; j < kEmitItems; ++j) {
+    const uint32_t idx = first + j;
+    gid[j] = 0;
+    cnt[j] = 0;
+    if (idx < n) {
+      const uint32_t g = order[idx];
+      if (g >= n) {
+        atomicOr(error, kErrIndex);
+        continue;
+      }
+      gid[j] = g;
+      const int32_t *tl = rect_tl + (size_t)g * rect_stride;
+      const int32_t *br = rect_br + (size_t)g * rect_stride;
+      const long long c = counts ? (long long)max(counts[g], 0) : rect_count(tl, br);
+      cnt[j] = c;
+      mysum += (unsigned long long)c;
+    }
+  }
+  unsigned long long block_total;
+  const unsigned long long excl =
+      block_exclusive_scan<unsigned long long>(mysum, s_tmp, &block_total);
+  if (t == 0) {
+    unsigned long long prev = 0;
+    unsigned long long *mine = status + chunk;
+    if (chunk == 0) {
+      st_volatile64(mine, kFlag64Prefix | block_total);
+    } else {
+      st_volatile64(mine, kFlag64Agg | block_total);
+      int64_t c = (int64_t)chunk - 1;
+      uint32_t spins = 0;
+      while (c >= 0) {
+        const unsigned long long sv = ld_volatile64(status + c);
+        const unsigned long long flag = sv & ~kCount64Mask;
+        if (flag == 0ull) {
+          if (++spins > kSpinLimit) {
+            atomicOr(error, kErrTimeout);
+            break;
+          }
+          __nanosleep(32);
+          continue;
+        }
+        prev += sv & kCount64Mask;
+        if (flag == kFlag64Prefix) break;
+        --c;
+      }
+      st_volatile64(mine, kFlag64Prefix | (prev + block_total));
+    }
+    s_prefix = prev;
+    if ((unsigned long long)(chunk + 1) * kEmitTile >= n) *total_out = prev + block_total;
+  }
+  __syncthreads();
+  unsigned long long off = s_prefix + excl;
+#pragma unroll 1
+  for (int j = 0; j < kEmitItems; ++j) {
+    if (cnt[j] == 0) continue;
+    const uint32_t g = gid[j];
+    const int32_t *tl = rect_tl + (size_t)g * rect_stride;
+    const int32_t *br = rect_br + (size_t)g * rect_stride;
+    if (rect_count(tl, br) != cnt[j]) atomicOr(error, kErrCount);
+    const bool in_grid = tl[0] >= 0 && tl[1] >= 0 && br[0] < n_tiles_w && br[1] < n_tiles_h;
+    if (!in_grid) atomicOr(error, kErrRange);
+    if (off >= capacity) break;  // the count is known from the scan; nothing more fits
+    const unsigned long long stop =
+        off + (unsigned long long)cnt[j] < capacity ? off + (unsigned long long)cnt[j] : capacity;
+    for (int32_t y = tl[1]; y <= br[1] && off < stop; ++y)
+      for (int32_t x = tl[0]; x <= br[0] && off < stop; ++x) {
+        tile_out[off] = in_grid ? (uint32_t)(y * n_tiles_w + x) : 0xffffffffu;
+        id_out[off] = g;
+        ++off;
+      }
+    off = s_prefix + excl;  // recompute the running offset from the counts
+    for (int jj = 0; jj <= j; ++jj) off += (unsigned long long)cnt[jj];
+  }
+}
+
+__global__ void ranges_kernel(const uint32_t *__restrict__ tiles, uint32_t K, uint32_t n_tiles,
+                              int32_t *__restrict__ start, int32_t *__restrict__ end) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K) return;
+  const uint32_t t = tiles[i];
+  if (t >= n_tiles) return;
+  if (i == 0 || tiles[i - 1] != t) start[t] = (int32_t)i;
+  if (i == K - 1 || tiles[i + 1] != t) end[t] = (int32_t)(i + 1);
+}
+
+inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+struct Workspace {
+  uint32_t *dkeys[2], *dvals[2];
+  uint32_t *tkeys[2], *tvals[2];
+  uint32_t *hist;      // [8][256]
+  uint32_t *status;    // [max_chunks][256]
+  unsigned long long *emit_status;
+  uint32_t *counters;  // [16]
+  uint32_t *error;
+  unsigned long long *total;
+  size_t status_words, emit_words;
+  size_t bytes;
+};
+
+Workspace carve_ws(void *base, int64_t n, int64_t cap) {
+  Workspace w;
+  char *p = static_cast<char *>(base);
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    char *r = p ? p + off : nullptr;
+    off += align256(bytes);
+    return r;
+  };
+  const size_t nn = (size_t)(n > 0 ? n : 1), cc = (size_t)(cap > 0 ? cap : 1);
+  for (int i = 0; i < 2; ++i) w.dkeys[i] = reinterpret_cast<uint32_t *>(take(4 * nn));
+  for (int i = 0; i < 2; ++i) w.dvals[i] = reinterpret_cast<uint32_t *>(take(4 * nn));
+  for (int i = 0; i < 2; ++i) w.tkeys[i] = reinterpret_cast<uint32_t *>(take(4 * cc));
+  for (int i = 0; i < 2; ++i) w.tvals[i] = reinterpret_cast<uint32_t *>(take(4 * cc));
+  w.hist = reinterpret_cast<uint32_t *>(take(8 * 256 * 4));
+  const size_t max_items = nn > cc ? nn : cc;
+  w.status_words = ((max_items + kTile - 1) / kTile) * 256;
+  w.status = reinterpret_cast<uint32_t *>(take(4 * w.status_words));
+  w.emit_words = (nn + kEmitTile - 1) / kEmitTile;
+  w.emit_status = reinterpret_cast<unsigned long long *>(take(8 * w.emit_words));
+  w.counters = reinterpret_cast<uint32_t *>(take(16 * 4));
+  w.error = reinterpret_cast<uint32_t *>(take(4));
+  w.total = reinterpret_cast<unsigned long long *>(take(8));
+  w.bytes = off;
+  return w;
+}
+
+// Stable LSD sort of n (key, value) pairs over `bits` low key bits.  The
+// final pass writes into (final_keys, final_vals); intermediate passes use
+// the two scratch buffers.  keys_in/vals_in are never written.
+int radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t n, int bits,
+               uint32_t *scratch_k[2], uint32_t *scratch_v[2], uint32_t *final_keys,
+               uint32_t *final_vals, const Workspace &w, cudaStream_t s) {
+  const int passes = (bits + 7) / 8;
+  if (n == 0 || passes == 0) return GSX_OK;
+  cudaError_t e = cudaMemsetAsync(w.hist, 0, 8 * 256 * 4, s);
+  if (e != cudaSuccess) return cuda_status(e, "memset histogram");
+  uint32_t hist_grid = (n + kThreads * 16 - 1) / (kThreads * 16);
+  if (hist_grid > 1024u) hist_grid = 1024u;
+  histogram_kernel<<<hist_grid, kThreads, 0, s>>>(keys_in, n, passes, w.hist);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_status(e, "histogram_kernel launch");
+  const uint32_t chunks = (n + kTile - 1) / kTile;
+  const uint32_t *ki = keys_in, *vi = vals_in;
+  for (int p = 0; p < passes; ++p) {
+    const bool last = p == passes - 1;
+    uint32_t *ko = last ? final_keys : scratch_k[p & 1];
+    uint32_t *vo = last ? final_vals : scratch_v[p & 1];
+    e = cudaMemsetAsync(w.status, 0, (size_t)chunks * 256 * 4, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(w.counters + p, 0, 4, s);
+    if (e != cudaSuccess) return cuda_status(e, "memset look-back status");
+    onesweep_kernel<<<chunks, kThreads, 0, s>>>(ki, vi, ko, vo, n, 8 * p, w.hist + 256 * p,
+                                                 w.status, w.counters + p, w.error);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_status(e, "onesweep_kernel launch");
+    ki = ko;
+    vi = vo;
+  }
+  return GSX_OK;
+}
+
+int bits_for(uint64_t max_value) {
+  int b = 0;
+  while (b < 32 && (max_value >> b) != 0) ++b;
+  return b;
+}
+
+}  // namespace
+
+size_t binning_workspace_bytes(int64_t n, int64_t cap, int64_t n_tiles) {
+  (void)n_tiles;
+  return carve_ws(nullptr, n, cap).bytes;
+}
+
+int run_binning(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
+                int32_t rect_stride, const int32_t *counts, const float *depth,
+                int32_t n_tiles_w, int32_t n_tiles_h, int64_t capacity, int32_t *ids,
+                int32_t *start, int32_t *end, int64_t *n_keys_host, void *ws,
+                size_t ws_bytes, cudaStream_t s) {
+  const int64_t n_tiles = (int64_t)n_tiles_w * n_tiles_h;
+  Workspace w = carve_ws(ws, n, capacity);
+  if (ws_bytes < w.bytes) {
+    set_error("binning workspace too small: %zu < %zu bytes", ws_bytes, w.bytes);
+    return GSX_ERR_CAPACITY;
+  }
+  cudaError_t e = cudaMemsetAsync(start, 0xff, sizeof(int32_t) * (size_t)n_tiles, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(end, 0xff, sizeof(int32_t) * (size_t)n_tiles, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.counters, 0, 16 * 4 + 0, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.error, 0, 4, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.total, 0, 8, s);
+  if (e != cudaSuccess) return cuda_status(e, "memset binning state");
+  if (n == 0) {
+    *n_keys_host = 0;
+    return GSX_OK;
+  }
+  const uint32_t nn = (uint32_t)n;
+  // 1. Gaussians sorted by depth bits (values = Gaussian index)
+  uint32_t *sk[2] = {w.dkeys[0], w.dkeys[1]}, *sv[2] = {w.dvals[0], w.dvals[1]};
+  int st = radix_sort(reinterpret_cast<const uint32_t *>(depth), nullptr, nn, 32, sk, sv,
+                      w.dkeys[1], w.dvals[1], w, s);
+  if (st != GSX_OK) return st;
+  // 2. scan of counts + emission
+  const uint32_t emit_chunks = (nn + kEmitTile - 1) / kEmitTile;
+  e = cudaMemsetAsync(w.emit_status, 0, 8 * (size_t)emit_chunks, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.counters + 8, 0, 4, s);
+  if (e != cudaSuccess) return cuda_status(e, "memset emission state");
+  emit_kernel<<<emit_chunks, kThreads, 0, s>>>(
+      w.dvals[1], nn, rect_tl, rect_br, rect_stride, counts, n_tiles_w, n_tiles_h, w.tkeys[0],
+      w.tvals[0], (unsigned long long)capacity, w.emit_status, w.counters + 8, w.total,
+      w.error);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_status(e, "emit_kernel launch");
+  unsigned long long total_h = 0;
+  uint32_t err_h = 0;
+  e = cudaMemcpyAsync(&total_h, w.total, 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&err_h, w.error, 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_status(e, "read key count");
+  *n_keys_host = (int64_t)total_h;
+  if (err_h & kErrTimeout) {
+    set_error("binning: a look-back wait expired (depth sort or key scan)");
+    return GSX_ERR_TIMEOUT;
+  }
+  if (err_h & kErrCount) {
+    set_error("binning: key counts disagree with the rectangles");
+    return GSX_ERR_MISMATCH;
+  }
+  if (err_h & kErrRange) {
+    set_error("binning: a rectangle lies outside the %d x %d tile grid", n_tiles_w, n_tiles_h);
+    return GSX_ERR_INVALID_ARG;
+  }
+  if (err_h & kErrIndex) {
+    set_error("binning: corrupted depth order");
+    return GSX_ERR_TIMEOUT;
+  }
+  if ((int64_t)total_h > capacity) {
+    set_error("binning: %llu keys exceed the capacity of %lld", total_h, (long long)capacity);
+    return GSX_ERR_CAPACITY;
+  }
+  const uint32_t K = (uint32_t)total_h;
+  if (K == 0) return GSX_OK;
+  // 3. stable sort by tile id.  Pass p writes tkeys[1] for even p and
+  // tkeys[0] for odd p; the last pass writes the ids into the caller's buffer
+  // and its keys into whichever tile buffer is not its input.
+  const int tile_bits = bits_for((uint64_t)(n_tiles - 1));
+  uint32_t *ids_u = reinterpret_cast<uint32_t *>(ids);
+  uint32_t *final_keys = w.tkeys[0];
+  if (tile_bits == 0) {
+    e = cudaMemcpyAsync(ids_u, w.tvals[0], 4 * (size_t)K, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return cuda_status(e, "copy ids");
+  } else {
+    const int passes = (tile_bits + 7) / 8;
+    uint32_t *tk[2] = {w.tkeys[1], w.tkeys[0]}, *tv[2] = {w.tvals[1], w.tvals[0]};
+    final_keys = (passes & 1) ? w.tkeys[1] : w.tkeys[0];
+    st = radix_sort(w.tkeys[0], w.tvals[0], K, tile_bits, tk, tv, final_keys, ids_u, w, s);
+    if (st != GSX_OK) return st;
+  }
+  // 4. start / end
+  ranges_kernel<<<(K + 255) / 256, 256, 0, s>>>(final_keys, K, (uint32_t)n_tiles, start, end);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_status(e, "ranges_kernel launch");
+  e = cudaMemcpyAsync(&err_h, w.error, 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_status(e, "read binning status");
+  if (err_h & kErrTimeout) {
+    set_error("binning: a look-back wait expired (tile sort)");
+    return GSX_ERR_TIMEOUT;
+  }
+  return GSX_OK;
+}
+
+}  // namespace gsx

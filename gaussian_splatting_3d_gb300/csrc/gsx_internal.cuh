@@ -1,0 +1,113 @@
+// gsx_internal.cuh -- device helpers shared by the sm_103a kernels.
+//
+// Arithmetic contract (every kernel is compiled with -fmad=false, so only the
+// fmaf() calls written here fuse; division and sqrtf are IEEE round-to-nearest,
+// denormals are kept):
+//   * gsx_expf: Cody-Waite reduction with a two-part ln2, degree-7 Taylor
+//     polynomial, 2^j through the exponent bits, +0 below -87.  The same
+//     operation sequence is restated in the CPU oracle, so the two agree bit
+//     for bit; it replaces the CUDA expf calls of the reference
+//     (gs/src/include/kernels.h:188, shencoder.h:4).
+//   * fmaf() sits where nvcc contracts the reference's a*b+c expressions.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/gsx.h"
+
+namespace gsx {
+
+constexpr float kMinRenderAlpha = 1.0f / 255.0f;  // gs/src/include/common.h:89
+
+__device__ __forceinline__ float gsx_expf(float x) {
+  if (!(x > -87.0f)) return (x != x) ? x : 0.0f;
+  if (x > 88.75f) return __int_as_float(0x7f800000);
+  float t = fmaf(x, 1.44269502162933349609375f, 12582912.0f);
+  float j = t - 12582912.0f;
+  float r = fmaf(j, -0.693145751953125f, x);
+  r = fmaf(j, -1.428606765330187045e-06f, r);
+  float p = 1.98412698412698412e-04f;
+  p = fmaf(p, r, 1.38888888888888889e-03f);
+  p = fmaf(p, r, 8.33333333333333333e-03f);
+  p = fmaf(p, r, 4.16666666666666667e-02f);
+  p = fmaf(p, r, 1.66666666666666667e-01f);
+  p = fmaf(p, r, 0.5f);
+  p = fmaf(p, r, 1.0f);
+  p = fmaf(p, r, 1.0f);
+  int ji = (int)j;
+  if (ji > 127) {
+    p = p * 2.0f;
+    ji -= 1;
+  }
+  return p * __int_as_float((ji + 127) << 23);
+}
+
+__device__ __forceinline__ float gsx_sigmoidf(float x) {
+  return 1.0f / (1.0f + gsx_expf(-x));
+}
+
+// float -> int32 truncation with saturation and NaN -> 0 (cvt.rzi.s32.f32).
+__device__ __forceinline__ int32_t f2i_sat(float f) { return __float2int_rz(f); }
+
+// Sphere-vs-frustum test of gs/src/include/kernels.h:156-170.
+__device__ __forceinline__ bool sphere_in_frustum(float mx, float my, float mz,
+                                                  float r, const float *normals,
+                                                  const float *pts) {
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    float dx = mx - pts[3 * i], dy = my - pts[3 * i + 1], dz = mz - pts[3 * i + 2];
+    float d = fmaf(dz, normals[3 * i + 2], fmaf(dy, normals[3 * i + 1], dx * normals[3 * i]));
+    if (!(d > -r)) return false;
+  }
+  return true;
+}
+
+// Host-side helpers (implemented in abi.cu).
+void set_error(const char *fmt, ...);
+int cuda_status(cudaError_t e, const char *what);
+
+// Launchers (each returns a GSX status).
+int launch_cull_bsphere(int64_t n, const float *mean, const float *svec,
+                        const float *normal, const float *pts, uint8_t *mask,
+                        float thresh, cudaStream_t s);
+int launch_project_forward(int64_t n, const float *mean, const float *qvec,
+                           const float *log_scale, const float *alpha_logit,
+                           const gsx_camera &cam, float frustum_radius,
+                           float tile_radius, int32_t tile_w, int32_t tile_h,
+                           int32_t scales_are_activated, float *mean2d,
+                           float *cov2d, float *depth, float *alpha, int32_t *rect,
+                           int32_t *counts, cudaStream_t s);
+int launch_project_backward(int64_t n, const float *mean, const float *qvec,
+                            const float *log_scale, const float *alpha_logit,
+                            const gsx_camera &cam, const int32_t *counts,
+                            const float *g_mean2d, const float *g_cov2d,
+                            const float *g_alpha, float *g_mean, float *g_qvec,
+                            float *g_logs, float *g_alpha_logit, cudaStream_t s);
+
+struct RasterArgs {
+  int64_t n, n_keys;  // Gaussians and list entries: bounds for start/end/ids
+  int32_t width, height, tile_w, tile_h, n_tiles_w, n_tiles_h;
+  int32_t sh_stride;
+  float psx, psy, T_thresh;
+  int32_t write_empty;
+  const float *mean2d, *cov2d, *sh, *alpha;
+  const int32_t *start, *end, *ids;
+  const float *topleft, *c2w;
+  float *out;
+  // backward only
+  const float *final_img, *grad_out;
+  float *g_mean2d, *g_cov2d, *g_sh, *g_alpha;
+};
+int launch_raster_forward(const RasterArgs &a, int C, cudaStream_t s);
+int launch_raster_backward(const RasterArgs &a, int C, cudaStream_t s);
+
+// Binning.  rect_tl/rect_br point at int32 pairs with `rect_stride` ints per
+// Gaussian (4 for packed [n,4] rects, 2 for separate [n,2] arrays).
+size_t binning_workspace_bytes(int64_t n, int64_t cap, int64_t n_tiles);
+int run_binning(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
+                int32_t rect_stride, const int32_t *counts, const float *depth,
+                int32_t n_tiles_w, int32_t n_tiles_h, int64_t capacity,
+                int32_t *ids, int32_t *start, int32_t *end, int64_t *n_keys_host,
+                void *ws, size_t ws_bytes, cudaStream_t s);
+
+}  // namespace gsx

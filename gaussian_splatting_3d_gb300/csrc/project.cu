@@ -1,0 +1,332 @@
+// project.cu -- per-Gaussian passes: bounding-sphere culling (drop-in), the
+// fused projection forward and its backward.
+//
+// Reference behaviour restated here:
+//   culling      gs/src/include/culling.h:11-20, kernels.h:156-170
+//   projection   gs/renderer.py:365-419 (project_pts, jacobian under no_grad,
+//                cov2d = (J W Sigma W^T J^T)[:2,:2], mean2d = p_xy / p_z)
+//   rotation     utils/transforms.py:31-45 (WXYZ quaternion normalised first,
+//                M = R diag(s), Sigma = M M^T)
+//   activations  utils/activations.py:13-19 (svec = exp, alpha = sigmoid)
+//   AABB / count gs/culling.py:8-37, utils/camera.py:290-303
+//
+// One thread per Gaussian; every output row is written by the thread that
+// owns it, so the pass is a single streaming read of 44 B and write of
+// 48 B per Gaussian.
+#include "gsx_internal.cuh"
+
+namespace gsx {
+
+namespace {
+
+__global__ void cull_bsphere_kernel(int64_t n, const float *__restrict__ mean,
+                                    const float *__restrict__ svec,
+                                    const float *__restrict__ normal,
+                                    const float *__restrict__ pts,
+                                    uint8_t *__restrict__ mask, float thresh) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float *s = svec + 3 * i;
+  float r = fmaxf(fmaxf(s[0], s[1]), s[2]) * thresh;
+  const float *m = mean + 3 * i;
+  mask[i] = sphere_in_frustum(m[0], m[1], m[2], r, normal, pts) ? 1 : 0;
+}
+
+struct ProjCam {
+  float W[3][3];  // W = R^T, W[i][j] = c2w[j][i]
+  float t[3];
+  float fx, fy, cx, cy;
+  int32_t width, height;
+  float normals[18], pts[18];
+};
+
+ProjCam make_proj_cam(const gsx_camera &c) {
+  ProjCam p;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) p.W[i][j] = c.c2w[4 * j + i];
+  p.t[0] = c.c2w[3];
+  p.t[1] = c.c2w[7];
+  p.t[2] = c.c2w[11];
+  p.fx = c.fx;
+  p.fy = c.fy;
+  p.cx = c.cx;
+  p.cy = c.cy;
+  p.width = c.width;
+  p.height = c.height;
+  for (int k = 0; k < 18; ++k) {
+    p.normals[k] = c.frustum_normals[k];
+    p.pts[k] = c.frustum_pts[k];
+  }
+  return p;
+}
+
+struct Rot {
+  float w, x, y, z;  // normalised quaternion
+  float R[3][3];
+};
+
+__device__ __forceinline__ void quat_rot(const float4 q, Rot &o) {
+  float n2 = fmaf(q.w, q.w, fmaf(q.z, q.z, fmaf(q.y, q.y, q.x * q.x)));
+  float nrm = fmaxf(sqrtf(n2), 1e-12f);
+  float w = q.x / nrm, x = q.y / nrm, y = q.z / nrm, z = q.w / nrm;
+  o.w = w;
+  o.x = x;
+  o.y = y;
+  o.z = z;
+  float tx = 2.0f * x, ty = 2.0f * y, tz = 2.0f * z;
+  float twx = tx * w, twy = ty * w, twz = tz * w;
+  float txx = tx * x, txy = ty * x, txz = tz * x;
+  float tyy = ty * y, tyz = tz * y, tzz = tz * z;
+  o.R[0][0] = 1.0f - (tyy + tzz);
+  o.R[0][1] = txy - twz;
+  o.R[0][2] = txz + twy;
+  o.R[1][0] = txy + twz;
+  o.R[1][1] = 1.0f - (txx + tzz);
+  o.R[1][2] = tyz - twx;
+  o.R[2][0] = txz - twy;
+  o.R[2][1] = tyz + twx;
+  o.R[2][2] = 1.0f - (txx + tyy);
+}
+
+__global__ void __launch_bounds__(256)
+    project_forward_kernel(int64_t n, const float *__restrict__ mean,
+                           const float4 *__restrict__ qvec,
+                           const float *__restrict__ log_scale,
+                           const float *__restrict__ alpha_logit, const ProjCam cam,
+                           float frustum_radius, float tile_radius, int32_t tile_w,
+                           int32_t tile_h, int32_t activated,
+                           float2 *__restrict__ mean2d, float4 *__restrict__ cov2d,
+                           float *__restrict__ depth, float *__restrict__ alpha,
+                           int4 *__restrict__ rect, int32_t *__restrict__ counts) {
+  int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n) return;
+  const float m0 = mean[3 * g], m1 = mean[3 * g + 1], m2 = mean[3 * g + 2];
+  float s0 = log_scale[3 * g], s1 = log_scale[3 * g + 1], s2 = log_scale[3 * g + 2];
+  if (!activated) {
+    s0 = gsx_expf(s0);
+    s1 = gsx_expf(s1);
+    s2 = gsx_expf(s2);
+  }
+  alpha[g] = alpha_logit ? gsx_sigmoidf(alpha_logit[g]) : 0.0f;
+  float r = fmaxf(fmaxf(s0, s1), s2) * frustum_radius;
+  if (!sphere_in_frustum(m0, m1, m2, r, cam.normals, cam.pts)) {
+    counts[g] = 0;
+    rect[g] = make_int4(0, 0, -1, -1);
+    mean2d[g] = make_float2(0.0f, 0.0f);
+    cov2d[g] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    depth[g] = 0.0f;
+    return;
+  }
+  // p = W (x - t)
+  float v0 = m0 - cam.t[0], v1 = m1 - cam.t[1], v2 = m2 - cam.t[2];
+  float p[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+    p[i] = fmaf(cam.W[i][2], v2, fmaf(cam.W[i][1], v1, cam.W[i][0] * v0));
+  Rot rot;
+  quat_rot(qvec[g], rot);
+  const float sv[3] = {s0, s1, s2};
+  float M[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) M[i][j] = sv[j] * rot.R[i][j];
+  float S[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      S[i][k] = fmaf(M[i][2], M[k][2], fmaf(M[i][1], M[k][1], M[i][0] * M[k][0]));
+  float iz = 1.0f / p[2];
+  float j02 = (-p[0] / p[2]) / p[2];
+  float j12 = (-p[1] / p[2]) / p[2];
+  float A[2][3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    A[0][k] = fmaf(j02, cam.W[2][k], iz * cam.W[0][k]);
+    A[1][k] = fmaf(j12, cam.W[2][k], iz * cam.W[1][k]);
+  }
+  float T[2][3];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      T[i][k] = fmaf(A[i][2], S[2][k], fmaf(A[i][1], S[1][k], A[i][0] * S[0][k]));
+  float cv[2][2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int l = 0; l < 2; ++l)
+      cv[i][l] = fmaf(T[i][2], A[l][2], fmaf(T[i][1], A[l][1], T[i][0] * A[l][0]));
+  float mx = p[0] / p[2], my = p[1] / p[2];
+  mean2d[g] = make_float2(mx, my);
+  cov2d[g] = make_float4(cv[0][0], cv[0][1], cv[1][0], cv[1][1]);
+  depth[g] = p[2];
+  float ax = sqrtf(tile_radius * cv[0][0]);
+  float ay = sqrtf(tile_radius * cv[1][1]);
+  float tlx = mx - ax, tly = my - ay, brx = mx + ax, bry = my + ay;
+  float ptlx = tlx * cam.fx + cam.cx, ptly = tly * cam.fy + cam.cy;
+  float pbrx = brx * cam.fx + cam.cx, pbry = bry * cam.fy + cam.cy;
+  int32_t itlx = min(max(f2i_sat(ptlx), 0), cam.width - 1) / tile_w;
+  int32_t itly = min(max(f2i_sat(ptly), 0), cam.height - 1) / tile_h;
+  int32_t ibrx = min(max(f2i_sat(pbrx), 0), cam.width - 1) / tile_w;
+  int32_t ibry = min(max(f2i_sat(pbry), 0), cam.height - 1) / tile_h;
+  rect[g] = make_int4(itlx, itly, ibrx, ibry);
+  counts[g] = (ibrx - itlx + 1) * (ibry - itly + 1);
+}
+
+// Parity-mode backward of the projection (depth detached, J constant).
+__global__ void __launch_bounds__(256)
+    project_backward_kernel(int64_t n, const float *__restrict__ mean,
+                            const float4 *__restrict__ qvec,
+                            const float *__restrict__ log_scale,
+                            const float *__restrict__ alpha_logit, const ProjCam cam,
+                            const int32_t *__restrict__ counts,
+                            const float2 *__restrict__ g_mean2d,
+                            const float4 *__restrict__ g_cov2d,
+                            const float *__restrict__ g_alpha,
+                            float *__restrict__ g_mean, float4 *__restrict__ g_qvec,
+                            float *__restrict__ g_logs,
+                            float *__restrict__ g_alpha_logit) {
+  int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n) return;
+  if (counts[g] == 0) {
+    g_mean[3 * g] = 0.0f;
+    g_mean[3 * g + 1] = 0.0f;
+    g_mean[3 * g + 2] = 0.0f;
+    g_logs[3 * g] = 0.0f;
+    g_logs[3 * g + 1] = 0.0f;
+    g_logs[3 * g + 2] = 0.0f;
+    g_qvec[g] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    g_alpha_logit[g] = 0.0f;
+    return;
+  }
+  const float m0 = mean[3 * g], m1 = mean[3 * g + 1], m2 = mean[3 * g + 2];
+  float v0 = m0 - cam.t[0], v1 = m1 - cam.t[1], v2 = m2 - cam.t[2];
+  float p[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+    p[i] = fmaf(cam.W[i][2], v2, fmaf(cam.W[i][1], v1, cam.W[i][0] * v0));
+  const float2 gm = g_mean2d[g];
+  const float gp0 = gm.x / p[2], gp1 = gm.y / p[2];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) g_mean[3 * g + j] = fmaf(cam.W[1][j], gp1, cam.W[0][j] * gp0);
+  float iz = 1.0f / p[2];
+  float j02 = (-p[0] / p[2]) / p[2];
+  float j12 = (-p[1] / p[2]) / p[2];
+  float A[2][3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    A[0][k] = fmaf(j02, cam.W[2][k], iz * cam.W[0][k]);
+    A[1][k] = fmaf(j12, cam.W[2][k], iz * cam.W[1][k]);
+  }
+  const float4 gc = g_cov2d[g];
+  // B = Gc A (2x3); GS = A^T B (3x3)
+  float B[2][3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    B[0][k] = fmaf(gc.y, A[1][k], gc.x * A[0][k]);
+    B[1][k] = fmaf(gc.w, A[1][k], gc.z * A[0][k]);
+  }
+  float GS[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) GS[i][k] = fmaf(A[1][i], B[1][k], A[0][i] * B[0][k]);
+  Rot rot;
+  quat_rot(qvec[g], rot);
+  float s[3];
+  s[0] = gsx_expf(log_scale[3 * g]);
+  s[1] = gsx_expf(log_scale[3 * g + 1]);
+  s[2] = gsx_expf(log_scale[3 * g + 2]);
+  float M[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) M[i][j] = s[j] * rot.R[i][j];
+  float GR[3][3];
+  float gsc[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      float acc = 0.0f;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) acc = fmaf(GS[i][k] + GS[k][i], M[k][j], acc);
+      GR[i][j] = acc * s[j];
+      gsc[j] = fmaf(acc, rot.R[i][j], gsc[j]);
+    }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) g_logs[3 * g + j] = gsc[j] * s[j];
+  const float w = rot.w, x = rot.x, y = rot.y, z = rot.z;
+  float gw = 2.0f * (-z * GR[0][1] + y * GR[0][2] + z * GR[1][0] - x * GR[1][2] -
+                     y * GR[2][0] + x * GR[2][1]);
+  float gx = 2.0f * (y * GR[0][1] + z * GR[0][2] + y * GR[1][0] - 2.0f * x * GR[1][1] -
+                     w * GR[1][2] + z * GR[2][0] + w * GR[2][1] - 2.0f * x * GR[2][2]);
+  float gy = 2.0f * (-2.0f * y * GR[0][0] + x * GR[0][1] + w * GR[0][2] + x * GR[1][0] +
+                     z * GR[1][2] - w * GR[2][0] + z * GR[2][1] - 2.0f * y * GR[2][2]);
+  float gz = 2.0f * (-2.0f * z * GR[0][0] - w * GR[0][1] + x * GR[0][2] + w * GR[1][0] -
+                     2.0f * z * GR[1][1] + y * GR[1][2] + x * GR[2][0] + y * GR[2][1]);
+  const float4 q = qvec[g];
+  float nq = sqrtf(fmaf(q.w, q.w, fmaf(q.z, q.z, fmaf(q.y, q.y, q.x * q.x))));
+  float4 gq;
+  if (nq > 1e-12f) {
+    float dp = gw * w + gx * x + gy * y + gz * z;
+    gq = make_float4((gw - dp * w) / nq, (gx - dp * x) / nq, (gy - dp * y) / nq,
+                     (gz - dp * z) / nq);
+  } else {
+    gq = make_float4(gw / 1e-12f, gx / 1e-12f, gy / 1e-12f, gz / 1e-12f);
+  }
+  g_qvec[g] = gq;
+  float a = gsx_sigmoidf(alpha_logit[g]);
+  g_alpha_logit[g] = g_alpha[g] * (a * (1.0f - a));
+}
+
+inline unsigned grid_for(int64_t n, int threads) {
+  return (unsigned)((n + threads - 1) / threads);
+}
+
+}  // namespace
+
+int launch_cull_bsphere(int64_t n, const float *mean, const float *svec,
+                        const float *normal, const float *pts, uint8_t *mask,
+                        float thresh, cudaStream_t s) {
+  if (n == 0) return GSX_OK;
+  cull_bsphere_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, mean, svec, normal, pts,
+                                                        mask, thresh);
+  return cuda_status(cudaGetLastError(), "cull_bsphere_kernel launch");
+}
+
+int launch_project_forward(int64_t n, const float *mean, const float *qvec,
+                           const float *log_scale, const float *alpha_logit,
+                           const gsx_camera &cam, float frustum_radius,
+                           float tile_radius, int32_t tile_w, int32_t tile_h,
+                           int32_t scales_are_activated, float *mean2d,
+                           float *cov2d, float *depth, float *alpha, int32_t *rect,
+                           int32_t *counts, cudaStream_t s) {
+  if (n == 0) return GSX_OK;
+  project_forward_kernel<<<grid_for(n, 256), 256, 0, s>>>(
+      n, mean, reinterpret_cast<const float4 *>(qvec), log_scale, alpha_logit,
+      make_proj_cam(cam), frustum_radius, tile_radius, tile_w, tile_h,
+      scales_are_activated, reinterpret_cast<float2 *>(mean2d),
+      reinterpret_cast<float4 *>(cov2d), depth, alpha, reinterpret_cast<int4 *>(rect),
+      counts);
+  return cuda_status(cudaGetLastError(), "project_forward_kernel launch");
+}
+
+int launch_project_backward(int64_t n, const float *mean, const float *qvec,
+                            const float *log_scale, const float *alpha_logit,
+                            const gsx_camera &cam, const int32_t *counts,
+                            const float *g_mean2d, const float *g_cov2d,
+                            const float *g_alpha, float *g_mean, float *g_qvec,
+                            float *g_logs, float *g_alpha_logit, cudaStream_t s) {
+  if (n == 0) return GSX_OK;
+  project_backward_kernel<<<grid_for(n, 256), 256, 0, s>>>(
+      n, mean, reinterpret_cast<const float4 *>(qvec), log_scale, alpha_logit,
+      make_proj_cam(cam), counts, reinterpret_cast<const float2 *>(g_mean2d),
+      reinterpret_cast<const float4 *>(g_cov2d), g_alpha, g_mean,
+      reinterpret_cast<float4 *>(g_qvec), g_logs, g_alpha_logit);
+  return cuda_status(cudaGetLastError(), "project_backward_kernel launch");
+}
+
+}  // namespace gsx

@@ -1,0 +1,318 @@
+"""Differentiable rendering on the sm_103a kernels.
+
+Two autograd entry points:
+
+``render_sh`` -- the reference's ``_render_sh.apply`` (gs/renderer.py:672-828)
+    with the same 18 positional arguments, running the raster forward and
+    backward through this package's ``_gs`` functions.
+
+``rasterize`` / ``FusedRender`` -- the fused native path behind ``SHRenderer``:
+    projection (cull + EWA covariance + AABB count, one kernel), deterministic
+    tile binning, raster forward; backward = raster backward + projection
+    backward (parity mode: depth detached and J constant, exactly the
+    derivative the reference's autograd takes, gs/renderer.py:365-419).  The
+    projection is recomputed in the backward from the parameters, so only the
+    2D record (mean2d, cov2d, alpha), the key lists and the image are kept
+    between the passes.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _gs, _lib
+from ._lib import GsxRasterParams
+from ._torch import check_tensor, ptr, stream_handle
+from .camera import CameraInfo, make_gsx_camera
+
+
+class _render_sh(torch.autograd.Function):
+    """Mirror of gs/renderer.py:672-828 on the drop-in ``_gs`` functions."""
+
+    @staticmethod
+    def forward(ctx, mean, cov, sh_coeffs, alpha, start, end, gaussian_ids, topleft, c2w, tile_size,
+                n_tiles_h, n_tiles_w, pixel_size_x, pixel_size_y, H, W, C, thresh):
+        out = torch.zeros([H * W * 3], dtype=torch.float32, device=mean.device)
+        _gs.tile_based_vol_rendering_sh(mean, cov, sh_coeffs, alpha, start, end, gaussian_ids, out,
+                                        topleft, c2w, tile_size, n_tiles_h, n_tiles_w, pixel_size_x,
+                                        pixel_size_y, H, W, C, thresh)
+        ctx.save_for_backward(mean, cov, sh_coeffs, alpha, start, end, gaussian_ids, out, topleft, c2w)
+        ctx.const = [tile_size, n_tiles_h, n_tiles_w, pixel_size_x, pixel_size_y, H, W, C, thresh]
+        return out
+
+    @staticmethod
+    def backward(ctx, grad):
+        mean, cov, sh_coeffs, alpha, start, end, gaussian_ids, out, topleft, c2w = ctx.saved_tensors
+        grad_mean = torch.zeros_like(mean)
+        grad_cov = torch.zeros_like(cov)
+        grad_sh_coeffs = torch.zeros_like(sh_coeffs)
+        grad_alpha = torch.zeros_like(alpha)
+        _gs.tile_based_vol_rendering_backward_sh(mean, cov, sh_coeffs, alpha, start, end, gaussian_ids,
+                                                 out, grad_mean, grad_cov, grad_sh_coeffs, grad_alpha,
+                                                 grad.contiguous(), topleft, c2w, *ctx.const)
+        return (grad_mean, grad_cov, grad_sh_coeffs, grad_alpha) + (None,) * 14
+
+
+render_sh = _render_sh.apply
+
+
+@dataclass
+class RasterSettings:
+    """Renderer options with the reference's defaults (conf/garden_sh.yaml:19-36)."""
+
+    tile_w: int = 16
+    tile_h: int = 16
+    frustum_culling_radius: float = 1.0
+    tile_culling_radius: float = 6.0
+    T_thresh: float = 0.01
+    sh_order: int | None = None  # C used for colour (now_C); None = all coefficients
+
+    def tiles(self, cam: CameraInfo):
+        return (cam.w + self.tile_w - 1) // self.tile_w, (cam.h + self.tile_h - 1) // self.tile_h
+
+
+class BinningBuffers:
+    """Reusable device buffers for the key lists of one device (grow-only)."""
+
+    def __init__(self, device: torch.device):
+        self.device = device
+        self.capacity = 0
+        self.n = -1
+        self.ws = None
+        self.ids = None
+
+    def ensure(self, n: int, capacity: int, n_tiles: int):
+        if capacity > self.capacity or n != self.n or self.ws is None:
+            cap = max(capacity, self.capacity)
+            ws_bytes = _lib.load().gsx_binning_workspace_bytes(n, cap, n_tiles)
+            self.ws = torch.empty(ws_bytes, dtype=torch.uint8, device=self.device)
+            self.ids = torch.empty(max(cap, 1), dtype=torch.int32, device=self.device)
+            self.capacity = cap
+            self.n = n
+        return self
+
+
+_buffers: dict = {}
+
+
+def _bin_buffers(device) -> BinningBuffers:
+    key = (device.type, device.index)
+    if key not in _buffers:
+        _buffers[key] = BinningBuffers(device)
+    return _buffers[key]
+
+
+@dataclass
+class Projected:
+    mean2d: torch.Tensor
+    cov2d: torch.Tensor
+    depth: torch.Tensor
+    alpha: torch.Tensor
+    rect: torch.Tensor
+    counts: torch.Tensor
+
+
+def project(mean, qvec, log_scale, alpha_logit, gcam, settings: RasterSettings,
+            scales_are_activated: bool = False) -> Projected:
+    n = mean.shape[0]
+    dev = mean.device
+    pr = Projected(
+        torch.empty((n, 2), dtype=torch.float32, device=dev),
+        torch.empty((n, 4), dtype=torch.float32, device=dev),
+        torch.empty((n,), dtype=torch.float32, device=dev),
+        torch.empty((n,), dtype=torch.float32, device=dev),
+        torch.empty((n, 4), dtype=torch.int32, device=dev),
+        torch.empty((n,), dtype=torch.int32, device=dev),
+    )
+    _lib.call("gsx_project_forward", n, ptr(mean), ptr(qvec), ptr(log_scale), ptr(alpha_logit),
+              ctypes.byref(gcam), float(settings.frustum_culling_radius), float(settings.tile_culling_radius),
+              int(settings.tile_w), int(settings.tile_h), int(bool(scales_are_activated)), ptr(pr.mean2d),
+              ptr(pr.cov2d), ptr(pr.depth), ptr(pr.alpha), ptr(pr.rect), ptr(pr.counts), stream_handle(dev))
+    return pr
+
+
+def bin_gaussians(pr: Projected, n_tiles_w: int, n_tiles_h: int, key_hint: int | None = None):
+    """Sorted Gaussian ids per tile: returns (ids[K], start[T], end[T], K)."""
+    n = pr.counts.shape[0]
+    dev = pr.counts.device
+    T = n_tiles_w * n_tiles_h
+    buf = _bin_buffers(dev)
+    cap = max(buf.capacity, key_hint or 0, 4 * n, 1 << 16)
+    start = torch.empty((T,), dtype=torch.int32, device=dev)
+    end = torch.empty((T,), dtype=torch.int32, device=dev)
+    for _ in range(3):
+        buf.ensure(n, cap, T)
+        k = ctypes.c_int64(0)
+        st = _lib.load().gsx_bin_gaussians(n, ptr(pr.rect), ptr(pr.counts), ptr(pr.depth), n_tiles_w, n_tiles_h,
+                                           buf.capacity, ptr(buf.ids), ptr(start), ptr(end), ctypes.byref(k),
+                                           ptr(buf.ws), buf.ws.numel(), stream_handle(dev))
+        if st == _lib.GSX_ERR_CAPACITY and k.value > buf.capacity:
+            cap = int(k.value * 1.25) + 1024
+            continue
+        _lib.check(st, "gsx_bin_gaussians")
+        K = int(k.value)
+        return buf.ids[:K].clone() if K > 0 else buf.ids[:0].clone(), start, end, K
+    raise _lib.GsxCapacityError(_lib.GSX_ERR_CAPACITY, "gsx_bin_gaussians", "could not size the key buffer")
+
+
+def _raster_params(cam: CameraInfo, settings: RasterSettings, C: int, sh_stride: int) -> GsxRasterParams:
+    ntw, nth = settings.tiles(cam)
+    p = GsxRasterParams()
+    p.width, p.height = int(cam.w), int(cam.h)
+    p.tile_w, p.tile_h = int(settings.tile_w), int(settings.tile_h)
+    p.n_tiles_w, p.n_tiles_h = int(ntw), int(nth)
+    p.sh_order, p.sh_stride = int(C), int(sh_stride)
+    p.pixel_size_x, p.pixel_size_y = float(1.0 / cam.fx), float(1.0 / cam.fy)
+    p.T_thresh = float(settings.T_thresh)
+    p.write_empty_tiles = 1
+    return p
+
+
+class ViewPipeline:
+    """One view through the fused native path with persistent device buffers.
+
+    ``forward`` runs projection, binning and the raster forward and returns a
+    state object; ``backward`` runs the raster backward and the projection
+    backward from dL/dimage.  When ``timer`` is given, CUDA events bracket
+    each stage on the launching stream (names: project, binning, raster_fwd,
+    raster_bwd, project_bwd)."""
+
+    def __init__(self, device=None):
+        self.device = torch.device(device or "cuda")
+
+    def forward(self, mean, qvec, log_scale, sh, alpha_logit, c2w_np, cam: CameraInfo,
+                settings: RasterSettings, timer=None):
+        dev = mean.device
+        n = mean.shape[0]
+        sh_stride = sh.shape[-1]
+        C = settings.sh_order or int(round(sh_stride ** 0.5))
+        gcam = make_gsx_camera(c2w_np, cam)
+        ev = timer.stage if timer is not None else (lambda name: _null_ctx())
+        with ev("project"):
+            pr = project(mean, qvec, log_scale, alpha_logit, gcam, settings)
+        ntw, nth = settings.tiles(cam)
+        with ev("binning"):
+            ids, start, end, K = bin_gaussians(pr, ntw, nth)
+        topleft = torch.tensor(cam.topleft(), dtype=torch.float32).to(dev, non_blocking=True)
+        c2w_dev = torch.from_numpy(np.ascontiguousarray(c2w_np, dtype=np.float32)).reshape(3, 4).to(
+            dev, non_blocking=True)
+        out = torch.empty((cam.h, cam.w, 3), dtype=torch.float32, device=dev)
+        params = _raster_params(cam, settings, C, sh_stride)
+        with ev("raster_fwd"):
+            _lib.call("gsx_render_forward", ctypes.byref(params), n, K, ptr(pr.mean2d), ptr(pr.cov2d), ptr(sh),
+                      ptr(pr.alpha), ptr(start), ptr(end), ptr(ids), ptr(topleft), ptr(c2w_dev), ptr(out),
+                      stream_handle(dev))
+        return dict(pr=pr, ids=ids, start=start, end=end, K=K, topleft=topleft, c2w_dev=c2w_dev, out=out,
+                    params=params, gcam=gcam)
+
+    def backward(self, state, mean, qvec, log_scale, sh, alpha_logit, grad_out, timer=None):
+        dev = mean.device
+        n = mean.shape[0]
+        pr = state["pr"]
+        ev = timer.stage if timer is not None else (lambda name: _null_ctx())
+        grad_out = grad_out.contiguous()
+        g_mean2d = torch.zeros((n, 2), dtype=torch.float32, device=dev)
+        g_cov2d = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+        g_alpha = torch.zeros((n,), dtype=torch.float32, device=dev)
+        g_sh = torch.zeros_like(sh)
+        with ev("raster_bwd"):
+            _lib.call("gsx_render_backward", ctypes.byref(state["params"]), n, state["K"], ptr(pr.mean2d),
+                      ptr(pr.cov2d), ptr(sh), ptr(pr.alpha), ptr(state["start"]), ptr(state["end"]),
+                      ptr(state["ids"]), ptr(state["topleft"]), ptr(state["c2w_dev"]), ptr(state["out"]),
+                      ptr(grad_out), ptr(g_mean2d), ptr(g_cov2d), ptr(g_sh), ptr(g_alpha), stream_handle(dev))
+        g_mean = torch.empty_like(mean)
+        g_q = torch.empty_like(qvec)
+        g_ls = torch.empty_like(log_scale)
+        g_al = torch.empty_like(alpha_logit)
+        with ev("project_bwd"):
+            _lib.call("gsx_project_backward", n, ptr(mean), ptr(qvec), ptr(log_scale), ptr(alpha_logit),
+                      ctypes.byref(state["gcam"]), ptr(pr.counts), ptr(g_mean2d), ptr(g_cov2d), ptr(g_alpha),
+                      ptr(g_mean), ptr(g_q), ptr(g_ls), ptr(g_al), stream_handle(dev))
+        return g_mean, g_q, g_ls, g_sh, g_al
+
+
+class _null_ctx:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+
+class StageTimer:
+    """CUDA events around pipeline stages on the current stream; durations
+    are read after a synchronize."""
+
+    def __init__(self):
+        self.records = []  # (name, start_event, end_event)
+
+    def stage(self, name):
+        timer = self
+
+        class _Ctx:
+            def __enter__(self):
+                self.s = torch.cuda.Event(enable_timing=True)
+                self.e = torch.cuda.Event(enable_timing=True)
+                self.s.record()
+                return self
+
+            def __exit__(self, *a):
+                self.e.record()
+                timer.records.append((name, self.s, self.e))
+                return False
+
+        return _Ctx()
+
+    def summary(self):
+        torch.cuda.synchronize()
+        out = {}
+        for name, s, e in self.records:
+            out.setdefault(name, []).append(s.elapsed_time(e))
+        return {k: dict(mean_ms=float(np.mean(v)), count=len(v)) for k, v in out.items()}
+
+
+_pipelines: dict = {}
+
+
+def _pipeline(device) -> ViewPipeline:
+    key = (device.type, device.index)
+    if key not in _pipelines:
+        _pipelines[key] = ViewPipeline(device)
+    return _pipelines[key]
+
+
+class FusedRender(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, mean, qvec, log_scale, sh, alpha_logit, c2w_np, cam, settings):
+        for x, name in ((mean, "mean"), (qvec, "qvec"), (log_scale, "log_scale"), (sh, "sh_coeffs"),
+                        (alpha_logit, "alpha_logit")):
+            check_tensor(x, name)
+        pipe = _pipeline(mean.device)
+        state = pipe.forward(mean, qvec, log_scale, sh, alpha_logit, c2w_np, cam, settings)
+        ctx.save_for_backward(mean, qvec, log_scale, sh, alpha_logit)
+        ctx.state = state
+        ctx.pipe = pipe
+        return state["out"]
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        mean, qvec, log_scale, sh, alpha_logit = ctx.saved_tensors
+        grads = ctx.pipe.backward(ctx.state, mean, qvec, log_scale, sh, alpha_logit, grad_out)
+        ctx.state = None
+        return grads + (None, None, None)
+
+
+def rasterize(mean, qvec, log_scale, sh_coeffs, alpha_logit, c2w, cam: CameraInfo,
+              settings: RasterSettings | None = None) -> torch.Tensor:
+    """Render one view: parameters as in SHRenderer (log-scales, opacity
+    logits, SH [N,3,C_max^2]) and a [3,4] camera-to-world (host array or
+    tensor).  Returns the [H,W,3] image; differentiable w.r.t. all five
+    parameter tensors."""
+    settings = settings or RasterSettings()
+    if isinstance(c2w, torch.Tensor):
+        c2w = c2w.detach().to("cpu", torch.float32).numpy()
+    return FusedRender.apply(mean, qvec, log_scale, sh_coeffs, alpha_logit, np.asarray(c2w, np.float32), cam,
+                             settings)

@@ -1,0 +1,217 @@
+/*
+ * gsx.h -- C ABI of the GB300 (sm_103a) Gaussian-splatting rasteriser.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream
+ * (cudaStream_t passed as void*; NULL = legacy default stream) and returns an
+ * int status (GSX_OK = 0).  No entry point exits the process, traps on the
+ * device or allocates device memory: scratch space is passed in by the caller
+ * (size from the matching *_workspace_bytes query).  Unless stated otherwise a
+ * call only enqueues work on `stream` and returns without synchronising.
+ *
+ * Two groups of entry points:
+ *  1. the four hot-path functions of the reference's pybind module `_gs`
+ *     (gs/src/bindings.cpp:6-7, 29, 42-48), with the same argument order and
+ *     meaning and the same in-place output convention;
+ *  2. the fused native path used by gaussian_splatting_3d_gb300's renderer:
+ *     projection (cull + EWA + AABB count), deterministic tile binning,
+ *     the raster forward and backward with a per-channel SH stride, and the
+ *     projection backward.
+ */
+#ifndef GSX_H
+#define GSX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  GSX_OK = 0,
+  GSX_ERR_INVALID_ARG = 1, /* bad size, null pointer, unsupported option */
+  GSX_ERR_CAPACITY = 2,    /* caller-provided buffer or workspace too small */
+  GSX_ERR_TIMEOUT = 3,     /* a bounded device-side wait gave up */
+  GSX_ERR_CUDA = 4,        /* a CUDA runtime call failed */
+  GSX_ERR_MISMATCH = 5     /* inputs disagree with a caller-stated size */
+};
+
+/* Human-readable name of a status code. */
+const char *gsx_status_string(int status);
+/* Detail message of the last failing call on this host thread ("" if none). */
+const char *gsx_last_error(void);
+/* ABI version of this library (increments on any signature change). */
+int gsx_abi_version(void);
+
+/* ---- 1. reference `_gs` hot-path entry points --------------------------- */
+
+/*
+ * Replaces `culling_gaussian_bsphere` (gs/src/render.cu:15-43; kernel
+ * gs/src/include/culling.h:11-20).  mask[i] = 1 iff the sphere at mean[i]
+ * with radius max(svec[i]) * thresh is on or in front of all six planes
+ * (normal[6,3], pts[6,3]).  qvec is accepted and unused, as in the reference.
+ */
+int gsx_culling_gaussian_bsphere(int64_t n, const float *mean, const float *qvec,
+                                 const float *svec, const float *normal,
+                                 const float *pts, uint8_t *mask, float thresh,
+                                 void *stream);
+
+/*
+ * Workspace for gsx_tile_culling_aabb_start_end and gsx_bin_gaussians:
+ * n_gaussians Gaussians, up to key_capacity (tile, Gaussian) keys, n_tiles tiles.
+ */
+size_t gsx_binning_workspace_bytes(int64_t n_gaussians, int64_t key_capacity,
+                                   int64_t n_tiles);
+
+/*
+ * Replaces `tile_culling_aabb_start_end` (gs/src/render.cu:380-397;
+ * gs/src/include/aabb_culling.h:192-260).  aabb_topleft / aabb_bottomright
+ * are int32 [n,2] tile rectangles (inclusive), depth float [n].  Writes
+ * gaussian_ids[n_keys] sorted by (tile, depth bits) with equal keys in index
+ * order, and start/end[n_tiles_h*n_tiles_w] (-1 for tiles without keys).
+ * Like the reference it synchronises `stream` once, to check that the
+ * rectangles hold exactly n_keys keys (GSX_ERR_MISMATCH otherwise).
+ */
+int gsx_tile_culling_aabb_start_end(int64_t n, int64_t n_keys,
+                                    const int32_t *aabb_topleft,
+                                    const int32_t *aabb_bottomright,
+                                    const float *depth, int32_t n_tiles_h,
+                                    int32_t n_tiles_w, int32_t *gaussian_ids,
+                                    int32_t *start, int32_t *end, void *workspace,
+                                    size_t workspace_bytes, void *stream);
+
+/*
+ * Replaces `tile_based_vol_rendering_sh` (gs/src/render.cu:483-544; kernel
+ * gs/src/include/vol_render_sh.h:171-248).  mean f32[n,2], cov f32[n,2,2],
+ * sh_coeffs f32[n,3,C*C], alpha f32[n], start/end i32[n_tiles],
+ * gaussian_ids i32[n_keys], out f32[H*W*3] (pre-zeroed; pixels of empty
+ * tiles are left untouched), topleft f32[2] and c2w f32[3,4] in device
+ * memory.  C (SH order = degree + 1) in 1..4; tile_size*tile_size <= 1024.
+ */
+int gsx_tile_based_vol_rendering_sh(
+    int64_t n, int64_t n_keys, const float *mean, const float *cov,
+    const float *sh_coeffs, const float *alpha, const int32_t *start,
+    const int32_t *end, const int32_t *gaussian_ids, float *out,
+    const float *topleft, const float *c2w, uint32_t tile_size,
+    uint32_t n_tiles_h, uint32_t n_tiles_w, float pixel_size_x,
+    float pixel_size_y, uint32_t H, uint32_t W, uint32_t C, float thresh,
+    void *stream);
+
+/*
+ * Replaces `tile_based_vol_rendering_backward_sh` (gs/src/render.cu:546-624;
+ * kernel gs/src/include/vol_render_sh.h:353-455).  Same inputs as the
+ * forward plus out (the forward image) and grad_out f32[H*W*3]; adds into
+ * grad_mean f32[n,2], grad_cov f32[n,2,2] (slots 1 and 2 receive the same
+ * value), grad_sh_coeffs f32[n,3,C*C], grad_alpha f32[n] (pre-zeroed).
+ */
+int gsx_tile_based_vol_rendering_backward_sh(
+    int64_t n, int64_t n_keys, const float *mean, const float *cov,
+    const float *sh_coeffs, const float *alpha, const int32_t *start,
+    const int32_t *end, const int32_t *gaussian_ids, const float *out,
+    float *grad_mean, float *grad_cov, float *grad_sh_coeffs, float *grad_alpha,
+    const float *grad_out, const float *topleft, const float *c2w,
+    uint32_t tile_size, uint32_t n_tiles_h, uint32_t n_tiles_w,
+    float pixel_size_x, float pixel_size_y, uint32_t H, uint32_t W, uint32_t C,
+    float thresh, void *stream);
+
+/* ---- 2. fused native path ---------------------------------------------- */
+
+/* Pinhole camera; c2w is the [3,4] row-major camera-to-world matrix used by
+ * the reference (utils/camera.py:219-303); frustum planes as get_frustum
+ * returns them (normals normalised).  */
+typedef struct gsx_camera {
+  float c2w[12];
+  float fx, fy, cx, cy;
+  int32_t width, height;
+  float frustum_normals[18]; /* [6,3] */
+  float frustum_pts[18];     /* [6,3] */
+} gsx_camera;
+
+/*
+ * One pass over n Gaussians (mean f32[n,3], qvec f32[n,4] WXYZ,
+ * log_scale f32[n,3], alpha_logit f32[n]): scale = exp(log_scale),
+ * alpha = sigmoid(alpha_logit), bounding-sphere cull (radius factor
+ * frustum_radius), projection to normalised image coordinates with depth
+ * and J treated as the reference treats them (gs/renderer.py:365-419),
+ * the AABB tile rectangle (gs/culling.py:8-37 with tile_radius = D) and its
+ * key count.  Outputs: mean2d f32[n,2], cov2d f32[n,4], depth f32[n],
+ * alpha f32[n], rect i32[n,4] (tlx, tly, brx, bry), counts i32[n]
+ * (0 = culled).  If scales_are_activated != 0, log_scale holds exp(.) already.
+ */
+int gsx_project_forward(int64_t n, const float *mean, const float *qvec,
+                        const float *log_scale, const float *alpha_logit,
+                        const gsx_camera *cam, float frustum_radius,
+                        float tile_radius, int32_t tile_w, int32_t tile_h,
+                        int32_t scales_are_activated, float *mean2d, float *cov2d,
+                        float *depth, float *alpha, int32_t *rect,
+                        int32_t *counts, void *stream);
+
+/*
+ * Deterministic tile binning of n Gaussians from their rectangles
+ * (rect i32[n,4]), counts and depth: sort by depth bits, exclusive scan of
+ * counts in that order, key emission, stable sort by tile.  Results equal the
+ * reference's stable 64-bit sort of (tile << 32 | depth bits) keys with equal
+ * keys in index order.  Writes gaussian_ids[<= key_capacity], start/end
+ * (n_tiles_w*n_tiles_h, -1 = empty) and, on the host, *n_keys_out.
+ * Synchronises `stream` once to read the key count.  If the count exceeds
+ * key_capacity nothing past the count is written and GSX_ERR_CAPACITY is
+ * returned with *n_keys_out set, so the caller can grow and call again.
+ */
+int gsx_bin_gaussians(int64_t n, const int32_t *rect, const int32_t *counts,
+                      const float *depth, int32_t n_tiles_w, int32_t n_tiles_h,
+                      int64_t key_capacity, int32_t *gaussian_ids, int32_t *start,
+                      int32_t *end, int64_t *n_keys_out, void *workspace,
+                      size_t workspace_bytes, void *stream);
+
+/* Raster parameters of the fused path. */
+typedef struct gsx_raster_params {
+  int32_t width, height;
+  int32_t tile_w, tile_h;       /* tile_w*tile_h threads per tile, <= 1024 */
+  int32_t n_tiles_w, n_tiles_h;
+  int32_t sh_order;             /* C = SH degree + 1, 1..4 */
+  int32_t sh_stride;            /* floats per colour channel in sh (>= C*C) */
+  float pixel_size_x, pixel_size_y;
+  float T_thresh;
+  int32_t write_empty_tiles;    /* 1: write zeros for pixels of empty tiles */
+} gsx_raster_params;
+
+/* Forward raster over precomputed per-Gaussian mean2d/cov2d/alpha, SH
+ * coefficients sh f32[n,3,sh_stride]; topleft f32[2] and c2w f32[3,4] in
+ * device memory. */
+int gsx_render_forward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
+                       const float *mean2d, const float *cov2d, const float *sh,
+                       const float *alpha, const int32_t *start, const int32_t *end,
+                       const int32_t *gaussian_ids, const float *topleft,
+                       const float *c2w, float *out, void *stream);
+
+/* Backward raster; grad_* are added into (caller zeroes them). */
+int gsx_render_backward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
+                        const float *mean2d, const float *cov2d, const float *sh,
+                        const float *alpha, const int32_t *start,
+                        const int32_t *end, const int32_t *gaussian_ids,
+                        const float *topleft, const float *c2w, const float *out,
+                        const float *grad_out, float *grad_mean2d,
+                        float *grad_cov2d, float *grad_sh, float *grad_alpha,
+                        void *stream);
+
+/*
+ * Projection backward (parity mode: depth detached in mean2d = p_xy / p_z and
+ * J constant, as gs/renderer.py:365-419 does) from the raster gradients
+ * grad_mean2d f32[n,2], grad_cov2d f32[n,4], grad_alpha f32[n] to the
+ * parameter gradients grad_mean f32[n,3], grad_qvec f32[n,4],
+ * grad_log_scale f32[n,3], grad_alpha_logit f32[n] (overwritten; zero for
+ * culled Gaussians, i.e. counts[i] == 0).
+ */
+int gsx_project_backward(int64_t n, const float *mean, const float *qvec,
+                         const float *log_scale, const float *alpha_logit,
+                         const gsx_camera *cam, const int32_t *counts,
+                         const float *grad_mean2d, const float *grad_cov2d,
+                         const float *grad_alpha, float *grad_mean,
+                         float *grad_qvec, float *grad_log_scale,
+                         float *grad_alpha_logit, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GSX_H */

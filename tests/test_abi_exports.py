@@ -1,0 +1,59 @@
+"""The C-ABI library builds for sm_103a, loads without a GPU, and exports every
+entry point that include/gsx.h declares (no compute calls)."""
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+from gaussian_splatting_3d_gb300 import _build, _lib
+
+HEADER = Path(__file__).resolve().parents[1] / "include" / "gsx.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gsx_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    assert "gsx_tile_based_vol_rendering_sh" in names
+    assert "gsx_tile_culling_aabb_start_end" in names
+    assert len(names) >= 12
+
+
+def test_library_exports_every_declared_symbol():
+    path = _build.build()
+    lib = ctypes.CDLL(str(path))
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, f"not exported: {missing}"
+
+
+def test_python_binding_covers_header():
+    names = set(declared_functions())
+    bound = set(_lib.SIGNATURES)
+    assert names <= bound | {"gsx_binning_workspace_bytes"}, names - bound
+
+
+def test_status_strings_and_host_validation_without_gpu():
+    lib = _lib.load()
+    assert lib.gsx_abi_version() == 1
+    assert lib.gsx_status_string(0) == b"ok"
+    assert lib.gsx_status_string(2) == b"capacity exceeded"
+    # argument validation happens on the host before any CUDA call
+    st = lib.gsx_tile_based_vol_rendering_sh(10, 10, None, None, None, None, None, None, None, None, None, None,
+                                             16, 1, 1, 1.0, 1.0, 16, 16, 7, 0.01, None)
+    assert st == _lib.GSX_ERR_INVALID_ARG
+    assert b"SH order" in lib.gsx_last_error()
+    st = lib.gsx_bin_gaussians(-1, None, None, None, 1, 1, 0, None, None, None, None, None, 0, None)
+    assert st == _lib.GSX_ERR_INVALID_ARG
+    assert lib.gsx_binning_workspace_bytes(1000, 4000, 64) > 4 * 4000
+
+
+def test_workspace_size_grows_with_capacity():
+    lib = _lib.load()
+    a = lib.gsx_binning_workspace_bytes(1000, 1000, 64)
+    b = lib.gsx_binning_workspace_bytes(1000, 100000, 64)
+    assert b > a
