@@ -76,6 +76,10 @@ SIGNATURES = {
         c_int,
         [c_int64, c_int64, P, P, P, c_int32, c_int32, P, P, P, P, c_size_t, P],
     ),
+    "gsx_tile_culling_aabb_start_end_noalloc": (
+        c_int,
+        [c_int64, c_int64, P, P, P, c_int32, c_int32, P, P, P, P],
+    ),
     "gsx_tile_based_vol_rendering_sh": (
         c_int,
         [c_int64, c_int64, P, P, P, P, P, P, P, P, P, P,

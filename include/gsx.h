@@ -82,6 +82,28 @@ int gsx_tile_culling_aabb_start_end(int64_t n, int64_t n_keys,
                                     size_t workspace_bytes, void *stream);
 
 /*
+ * Same binning as gsx_tile_culling_aabb_start_end, for callers that cannot
+ * allocate device memory: a plugin inside another application's fixed
+ * memory budget, or a real-time loop that must never enter the allocator
+ * (cudaMalloc can synchronise the device).  It takes no workspace and
+ * allocates nothing; its scratch is a 64 MiB array in the library's static
+ * device memory, which every GPU that loads the library holds until the
+ * process exits.  Inputs whose scratch need exceeds 64 MiB (roughly
+ * 16 bytes per Gaussian plus 16 bytes per key) are rejected with
+ * GSX_ERR_CAPACITY.  The first call on each device looks up the array's
+ * device address; make that first call before any stream capture.  All calls
+ * share the array, so calls that overlap on the GPU (other streams, other
+ * host threads) race and must be serialised by the caller.  This entry point
+ * has no counterpart in the reference.
+ */
+int gsx_tile_culling_aabb_start_end_noalloc(int64_t n, int64_t n_keys,
+                                            const int32_t *aabb_topleft,
+                                            const int32_t *aabb_bottomright,
+                                            const float *depth, int32_t n_tiles_h,
+                                            int32_t n_tiles_w, int32_t *gaussian_ids,
+                                            int32_t *start, int32_t *end, void *stream);
+
+/*
  * Replaces `tile_based_vol_rendering_sh` (gs/src/render.cu:483-544; kernel
  * gs/src/include/vol_render_sh.h:171-248).  mean f32[n,2], cov f32[n,2,2],
  * sh_coeffs f32[n,3,C*C], alpha f32[n], start/end i32[n_tiles],
