@@ -102,18 +102,22 @@ def dist_env():
     return rank, world, local
 
 
-def algorithmic_bytes(stage, n, K, P, C, n_tiles, n_pairs_tg=None):
-    """Bytes a stage must move at minimum (per launch), as documented for the roofline."""
+def algorithmic_bytes(stage, n, K, P, C, n_tiles):
+    """Per-launch bytes of each stage, with the per-unit figures documented
+    for the roofline: per Gaussian for the projection passes, per key and per
+    pixel for the binning and raster passes."""
     CC = C * C
     if stage == "project":
         return n * (44 + 52)
     if stage == "binning":
-        # depth sort 4 passes (r+w key+value) + histogram, emission, tile sort 2 passes, ranges
-        return n * (4 * 16 + 4 + 4 + 20) + K * (8 + 2 * 16 + 4 + 4) + 8 * n_tiles
+        # depth sort: 4 passes x (8 B read + 8 B written) per Gaussian + histogram read;
+        # emission: 28 B per Gaussian + 8 B per key; tile sort: 2 passes x 16 B per key
+        # + histogram; ranges: 4 B per key + 8 B per tile
+        return n * (4 * 16 + 4 + 28) + K * (8 + 2 * 16 + 4 + 4) + 8 * n_tiles
     if stage == "raster_fwd":
-        return K * (32 + 12 * CC) + 12 * P
+        return K * (28 + 12 * CC) + 12 * P
     if stage == "raster_bwd":
-        return K * (32 + 12 * CC) + 36 * P + K * 4 * (6 + 3 * CC)
+        return K * (28 + 12 * CC) + 24 * P + K * 4 * (3 * CC + 7)
     if stage == "project_bwd":
         return n * (44 + 32 + 44)
     return 0
@@ -156,9 +160,12 @@ def run_gsx(args):
             dist.barrier()
         torch.cuda.synchronize()
 
+    from gaussian_splatting_3d_gb300 import _lib
+
     clocks = ClockSampler(local)
     timer = renderer.StageTimer()
     barrier()
+    launches0 = _lib.load().gsx_kernel_launch_count()
     clocks.start()
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
@@ -169,6 +176,7 @@ def run_gsx(args):
     t1.record()
     barrier()
     wall1 = time.perf_counter()
+    launches = int(_lib.load().gsx_kernel_launch_count() - launches0)
     clock_info = clocks.stop()
     ms = t0.elapsed_time(t1) / args.steps
     if world > 1:
@@ -248,7 +256,7 @@ def run_gsx(args):
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
                      "peak_source": f"{peaks_kind} hbm_gbs", "algorithmic_bytes": int(alg)},
         "clocks": clock_info,
-        "gpu_launches": None,
+        "gpu_launches": launches,
         "wall_s": round(wall1 - wall0, 3),
     }
     if not args.no_cpu_baseline:

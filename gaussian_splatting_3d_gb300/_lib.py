@@ -70,6 +70,7 @@ SIGNATURES = {
     "gsx_status_string": (c_char_p, [c_int]),
     "gsx_last_error": (c_char_p, []),
     "gsx_abi_version": (c_int, []),
+    "gsx_kernel_launch_count": (ctypes.c_uint64, []),
     "gsx_culling_gaussian_bsphere": (c_int, [c_int64, P, P, P, P, P, P, c_float, P]),
     "gsx_binning_workspace_bytes": (c_size_t, [c_int64, c_int64, c_int64]),
     "gsx_tile_culling_aabb_start_end": (

@@ -1,6 +1,7 @@
 // abi.cu -- the extern "C" entry points declared in include/gsx.h: argument
 // validation, status codes and a per-thread error message.  No entry point
 // exits the process or allocates device memory.
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -11,7 +12,10 @@ namespace gsx {
 
 namespace {
 thread_local char g_err[512] = {0};
+std::atomic<unsigned long long> g_launches{0};
 }
+
+void count_launches(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 void set_error(const char *fmt, ...) {
   va_list ap;
@@ -57,6 +61,8 @@ const char *gsx_status_string(int status) {
 const char *gsx_last_error(void) { return g_err; }
 
 int gsx_abi_version(void) { return 1; }
+
+uint64_t gsx_kernel_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 int gsx_culling_gaussian_bsphere(int64_t n, const float *mean, const float *qvec,
                                  const float *svec, const float *normal,

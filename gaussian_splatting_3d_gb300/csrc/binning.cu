@@ -386,6 +386,7 @@ int radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t n, int
   if (e != cudaSuccess) return cuda_status(e, "memset histogram");
   uint32_t hist_grid = (n + kThreads * 16 - 1) / (kThreads * 16);
   if (hist_grid > 1024u) hist_grid = 1024u;
+  count_launches(1);
   histogram_kernel<<<hist_grid, kThreads, 0, s>>>(keys_in, n, passes, w.hist);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_status(e, "histogram_kernel launch");
@@ -398,7 +399,8 @@ int radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t n, int
     e = cudaMemsetAsync(w.status, 0, (size_t)chunks * 256 * 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(w.counters + p, 0, 4, s);
     if (e != cudaSuccess) return cuda_status(e, "memset look-back status");
-    onesweep_kernel<<<chunks, kThreads, 0, s>>>(ki, vi, ko, vo, n, 8 * p, w.hist + 256 * p,
+    count_launches(1);
+  onesweep_kernel<<<chunks, kThreads, 0, s>>>(ki, vi, ko, vo, n, 8 * p, w.hist + 256 * p,
                                                  w.status, w.counters + p, w.error);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e, "onesweep_kernel launch");
@@ -453,6 +455,7 @@ int run_binning(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
   e = cudaMemsetAsync(w.emit_status, 0, 8 * (size_t)emit_chunks, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(w.counters + 8, 0, 4, s);
   if (e != cudaSuccess) return cuda_status(e, "memset emission state");
+  count_launches(1);
   emit_kernel<<<emit_chunks, kThreads, 0, s>>>(
       w.dvals[1], nn, rect_tl, rect_br, rect_stride, counts, n_tiles_w, n_tiles_h, w.tkeys[0],
       w.tvals[0], (unsigned long long)capacity, w.emit_status, w.counters + 8, w.total,
@@ -505,6 +508,7 @@ int run_binning(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
     if (st != GSX_OK) return st;
   }
   // 4. start / end
+  count_launches(1);
   ranges_kernel<<<(K + 255) / 256, 256, 0, s>>>(final_keys, K, (uint32_t)n_tiles, start, end);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_status(e, "ranges_kernel launch");

@@ -65,6 +65,8 @@ __device__ __forceinline__ bool sphere_in_frustum(float mx, float my, float mz,
 // Host-side helpers (implemented in abi.cu).
 void set_error(const char *fmt, ...);
 int cuda_status(cudaError_t e, const char *what);
+// Counts kernel launches issued by this library (read by gsx_kernel_launch_count).
+void count_launches(unsigned n);
 
 // Launchers (each returns a GSX status).
 int launch_cull_bsphere(int64_t n, const float *mean, const float *svec,
@@ -88,6 +90,7 @@ struct RasterArgs {
   int64_t n, n_keys;  // Gaussians and list entries: bounds for start/end/ids
   int32_t width, height, tile_w, tile_h, n_tiles_w, n_tiles_h;
   int32_t sh_stride;
+  int32_t batch;  // Gaussians per shared-memory batch (set by the launcher)
   float psx, psy, T_thresh;
   int32_t write_empty;
   const float *mean2d, *cov2d, *sh, *alpha;

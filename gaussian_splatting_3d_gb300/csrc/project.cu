@@ -292,6 +292,7 @@ int launch_cull_bsphere(int64_t n, const float *mean, const float *svec,
                         const float *normal, const float *pts, uint8_t *mask,
                         float thresh, cudaStream_t s) {
   if (n == 0) return GSX_OK;
+  count_launches(1);
   cull_bsphere_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, mean, svec, normal, pts,
                                                         mask, thresh);
   return cuda_status(cudaGetLastError(), "cull_bsphere_kernel launch");
@@ -305,6 +306,7 @@ int launch_project_forward(int64_t n, const float *mean, const float *qvec,
                            float *cov2d, float *depth, float *alpha, int32_t *rect,
                            int32_t *counts, cudaStream_t s) {
   if (n == 0) return GSX_OK;
+  count_launches(1);
   project_forward_kernel<<<grid_for(n, 256), 256, 0, s>>>(
       n, mean, reinterpret_cast<const float4 *>(qvec), log_scale, alpha_logit,
       make_proj_cam(cam), frustum_radius, tile_radius, tile_w, tile_h,
@@ -321,6 +323,7 @@ int launch_project_backward(int64_t n, const float *mean, const float *qvec,
                             const float *g_alpha, float *g_mean, float *g_qvec,
                             float *g_logs, float *g_alpha_logit, cudaStream_t s) {
   if (n == 0) return GSX_OK;
+  count_launches(1);
   project_backward_kernel<<<grid_for(n, 256), 256, 0, s>>>(
       n, mean, reinterpret_cast<const float4 *>(qvec), log_scale, alpha_logit,
       make_proj_cam(cam), counts, reinterpret_cast<const float2 *>(g_mean2d),

@@ -11,16 +11,31 @@
 //                         (final - out)/(1 - aG), 2D-Gaussian grads
 //                         (kernels.h:394-418), dL/dalpha = P * G
 //
-// GB300 layout: one CTA per tile, one thread per pixel.  Each batch of the
-// tile's sorted list is gathered once into shared memory (ids, mean, cov,
-// clamped alpha, SH rows padded to float4) and read by all threads as
-// broadcasts.  The CTA leaves the list as soon as every pixel has saturated
-// (__syncthreads_and on the per-pixel stop flag), which does not change any
-// pixel: a stopped pixel takes no further Gaussians in the reference either.
-// The backward reduces the per-pair gradients of a warp with a butterfly
-// reduce-scatter (one shuffle per value instead of five), folds the warps
-// together with shared-memory atomics, and issues one global atomic per
-// (tile, Gaussian, value).
+// GB300 layout: one CTA per tile, one thread per pixel, each warp an 8x4
+// block of pixels.  Each batch of the tile's sorted list is gathered once into
+// shared memory and compacted to the Gaussians whose conservative skip box
+// meets the tile; all threads then read the records as broadcasts.  A CTA
+// leaves the list as soon as every pixel has saturated (__syncthreads_and on
+// the per-pixel stop flag), which changes no pixel: a stopped pixel takes no
+// further Gaussian in the reference either.
+//
+// Arithmetic.  Everything that decides which pairs contribute -- the radial
+// distance, the exponential G (gsx_expf), a*G < 1/255, the transmittance T --
+// follows the operation sequence the CPU oracle restates, so those decisions
+// are bit-identical.  The colour path is a smooth function of its inputs and
+// uses the fast hardware forms: paired FMAs (two interleaved partial sums)
+// for the SH dot products and ex2/rcp for the sigmoid; images agree with the
+// oracle to ~1e-6.
+//
+// Backward.  Per contributing pair the thread forms the three SH weights
+// w_ch and six scalar gradients.  The scalars are summed over the warp with a
+// short butterfly.  The SH gradient of a Gaussian is the product
+// sum_p w_ch(p) Y_k(p) over the warp's 32 pixels, so each warp stages the
+// weights of up to five Gaussians as a 15x32 matrix and multiplies it with its
+// 32x16 basis matrix on the tensor cores (mma.sync m16n8k8, TF32 split into
+// high and low parts, three products, FP32 accumulation: ~2^-21 relative per
+// product).  Warp results meet in shared memory (atomics), and the CTA issues
+// one global atomic per (tile, Gaussian, value).
 #include "gsx_internal.cuh"
 
 namespace gsx {
@@ -34,11 +49,12 @@ struct Sh {
   static constexpr int CC = C * C;
   static constexpr int CCP = (CC + 3) & ~3;  // per-channel smem stride
   static constexpr int GSH = 3 * CCP;        // smem floats per Gaussian
+  static constexpr int NY2 = (CC + 1) / 2;   // basis as float2 pairs
 };
 
 template <int C>
-__device__ __forceinline__ void sh_basis(const float *__restrict__ c2w, float px,
-                                         float py, float *Y) {
+__device__ __forceinline__ void sh_basis(const float *__restrict__ c2w, float px, float py,
+                                         float *Y) {
   float d[3];
 #pragma unroll
   for (int r = 0; r < 3; ++r)
@@ -67,31 +83,38 @@ __device__ __forceinline__ void sh_basis(const float *__restrict__ c2w, float px
   Y[15] = (0.59004358992664352f * x) * fmaf(3.0f, y2, -x2);
 }
 
-// sum_k sh[k] * Y[k] as the reference's fused multiply-add chain.
+// sum_k sh[k] * Y[k] with paired FMAs over (even, odd) k; `s` is 16-byte
+// aligned, Y2[j] = (Y[2j], Y[2j+1]).
 template <int C>
-__device__ __forceinline__ float sh_dot(const float *__restrict__ s, const float *Y) {
+__device__ __forceinline__ float sh_logit(const float *__restrict__ s, const float2 *Y2) {
   constexpr int CC = C * C;
-  float acc = 0.0f;
-  if constexpr (CC % 4 == 0) {
-#pragma unroll
-    for (int k = 0; k < CC; k += 4) {
-      float4 q = *reinterpret_cast<const float4 *>(s + k);
-      acc = fmaf(q.x, Y[k], acc);
-      acc = fmaf(q.y, Y[k + 1], acc);
-      acc = fmaf(q.z, Y[k + 2], acc);
-      acc = fmaf(q.w, Y[k + 3], acc);
-    }
+  if constexpr (CC == 1) {
+    return s[0] * Y2[0].x;
   } else {
+    float2 acc = make_float2(0.0f, 0.0f);
 #pragma unroll
-    for (int k = 0; k < CC; ++k) acc = fmaf(s[k], Y[k], acc);
+    for (int k = 0; k + 3 < CC; k += 4) {
+      const float4 q = *reinterpret_cast<const float4 *>(s + k);
+      acc = __ffma2_rn(make_float2(q.x, q.y), Y2[k / 2], acc);
+      acc = __ffma2_rn(make_float2(q.z, q.w), Y2[k / 2 + 1], acc);
+    }
+    float r = acc.x + acc.y;
+    if constexpr (CC % 4 != 0) r = fmaf(s[CC - 1], Y2[CC / 2].x, r);  // CC = 9
+    return r;
   }
-  return acc;
 }
 
-// radial distance of gs/src/include/kernels.h:172-187 (before the exp).
-__device__ __forceinline__ float radial_of(float4 cv, float2 m, float px, float py) {
+__device__ __forceinline__ float fast_sigmoid(float x) {
+  float e, r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(x * -1.4426950408889634f));
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(1.0f + e));
+  return r;
+}
+
+// radial distance of gs/src/include/kernels.h:172-187 (before the exp), for
+// the pixel offset x = px - mean.x, y = py - mean.y.
+__device__ __forceinline__ float radial_of(float4 cv, float x, float y) {
   float det = fmaf(cv.x, cv.w, -(cv.y * cv.z));
-  float x = px - m.x, y = py - m.y;
   float tmpx = fmaf(x, cv.w, -(y * cv.z));
   float tmpy = fmaf(-x, cv.y, y * cv.x);
   float radial = fmaf(tmpx, x, tmpy * y);
@@ -116,73 +139,172 @@ __device__ __forceinline__ int tile_list_length(const RasterArgs &a, int tile, i
   return e - s0;
 }
 
+// Pixel of thread t: warps cover 8x4 blocks when the tile allows it (a
+// compact footprint means fewer warps per small Gaussian), else rows.
+__device__ __forceinline__ void pixel_of(const RasterArgs &a, int tile, int t, int &gx, int &gy) {
+  int lx, ly;
+  if ((a.tile_w & 7) == 0 && (a.tile_h & 3) == 0) {
+    const int w = t >> 5, l = t & 31, bpr = a.tile_w >> 3;
+    lx = (w % bpr) * 8 + (l & 7);
+    ly = (w / bpr) * 4 + (l >> 3);
+  } else {
+    lx = t % a.tile_w;
+    ly = t / a.tile_w;
+  }
+  gx = (tile % a.n_tiles_w) * a.tile_w + lx;
+  gy = (tile / a.n_tiles_w) * a.tile_h + ly;
+}
+
+// Normalised coordinates of the first and last pixel centres of a tile that
+// lie inside the image (computed like the pixel positions themselves).
+__device__ __forceinline__ void tile_bounds(const RasterArgs &a, int tile, float &x0, float &x1,
+                                            float &y0, float &y1) {
+  const int gx0 = (tile % a.n_tiles_w) * a.tile_w, gy0 = (tile / a.n_tiles_w) * a.tile_h;
+  const int gx1 = min(gx0 + a.tile_w, a.width) - 1, gy1 = min(gy0 + a.tile_h, a.height) - 1;
+  x0 = fmaf((float)gx0, a.psx, a.topleft[0]);
+  x1 = fmaf((float)gx1, a.psx, a.topleft[0]);
+  y0 = fmaf((float)gy0, a.psy, a.topleft[1]);
+  y1 = fmaf((float)gy1, a.psy, a.topleft[1]);
+  if (x0 > x1) { const float tmp = x0; x0 = x1; x1 = tmp; }
+  if (y0 > y1) { const float tmp = y0; y0 = y1; y1 = tmp; }
+}
+
 struct SmemLayout {
   float4 *cov;
   float2 *mean;
+  float2 *box;  // half-extents of the region where the pair may contribute
   float *alpha;
   int *ids;
   float *sh;
 };
 
+// Shared-memory layout of one batch of B Gaussians (B even): 10*B floats of
+// records followed by the SH rows, which start 16-byte aligned.
 template <int C>
 __device__ __forceinline__ SmemLayout carve(float *smem, int B) {
   SmemLayout L;
   L.cov = reinterpret_cast<float4 *>(smem);
   L.mean = reinterpret_cast<float2 *>(smem + 4 * B);
-  L.alpha = smem + 6 * B;
-  L.ids = reinterpret_cast<int *>(smem + 7 * B);
-  L.sh = smem + 8 * B;  // 32*B bytes from the base: float4 aligned
+  L.box = reinterpret_cast<float2 *>(smem + 6 * B);
+  L.alpha = smem + 8 * B;
+  L.ids = reinterpret_cast<int *>(smem + 9 * B);
+  L.sh = smem + 10 * B;
   return L;
 }
 
-// Gather one batch of the tile's list into shared memory.
+__device__ __forceinline__ float inf_f() { return __int_as_float(0x7f800000); }
+
+// Conservative skip region of one Gaussian.  With a = min(alpha, .99), a pair
+// is skipped by the reference when a * exp(-radial/2) < 1/255, i.e. whenever
+// radial > R_a = 2 ln(255 a).  For a well-conditioned covariance (both
+// diagonal entries positive, det > 1e-2 * c0 * c3, all finite) the float
+// radial differs from the exact quadratic form by far less than 1e-3
+// relative, so every pixel outside the ellipse x^T S^-1 x <= 1.01 R_a + 0.05
+// is skipped; that ellipse lies inside the box |dx| <= sqrt(R c0),
+// |dy| <= sqrt(R c3), widened by 1 % more.  drop = the Gaussian is skipped by
+// every pixel (a < 1/255 with a finite, non-negative G).  Anything else gets
+// an infinite box and takes the exact per-pixel path.
+__device__ __forceinline__ float2 skip_box(float4 cv, float2 m, float a, bool &drop) {
+  drop = false;
+  const bool finite = isfinite(cv.x) && isfinite(cv.y) && isfinite(cv.z) && isfinite(cv.w) &&
+                      isfinite(m.x) && isfinite(m.y);
+  const float det = fmaf(cv.x, cv.w, -(cv.y * cv.z));
+  const bool good = finite && cv.x > 0.0f && cv.w > 0.0f && det > 1e-2f * (cv.x * cv.w);
+  if (!good || !(a == a)) return make_float2(inf_f(), inf_f());
+  if (a < kMinRenderAlpha) {
+    drop = true;
+    return make_float2(0.0f, 0.0f);
+  }
+  const float R = fmaxf(2.0f * logf(255.0f * a), 0.0f) * 1.01f + 0.05f;
+  return make_float2(sqrtf(R * cv.x) * 1.01f + 1e-6f, sqrtf(R * cv.w) * 1.01f + 1e-6f);
+}
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned lt;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+  return lt;
+}
+
+// Gather one batch of the tile's list into shared memory, keeping only the
+// Gaussians whose skip box meets the tile's pixel centres (in list order).
+// Requires nb <= blockDim.x.  Returns the number kept.
 template <int C>
-__device__ __forceinline__ void load_batch(const RasterArgs &a, const SmemLayout &L,
-                                           int first, int nb, int t, int nthr) {
+__device__ __forceinline__ int load_batch(const RasterArgs &a, const SmemLayout &L, int first,
+                                          int nb, int t, int nthr, float tx0, float tx1,
+                                          float ty0, float ty1, int *s_wcount) {
   constexpr int CC = Sh<C>::CC, CCP = Sh<C>::CCP, GSH = Sh<C>::GSH;
-  for (int j = t; j < nb; j += nthr) {
-    const int id = a.ids[first + j];
+  const int lane = t & 31, warp = t >> 5, nwarps = nthr >> 5;
+  bool keep = false;
+  int id = -1;
+  float2 mm = make_float2(0.0f, 0.0f), box = make_float2(0.0f, 0.0f);
+  float4 cv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  float al = 0.0f;
+  if (t < nb) {
+    id = a.ids[first + t];
     if (id >= 0 && id < a.n) {
-      L.ids[j] = id;
       const float *m = a.mean2d + 2 * (int64_t)id;
-      const float *cv = a.cov2d + 4 * (int64_t)id;
-      L.mean[j] = make_float2(m[0], m[1]);
-      L.cov[j] = make_float4(cv[0], cv[1], cv[2], cv[3]);
-      L.alpha[j] = fminf(a.alpha[id], 0.99f);
-    } else {
-      // an id outside [0, n): a transparent Gaussian far off screen, skipped
-      // by every pixel (radial = inf), and no reads of the caller's arrays
-      L.ids[j] = -1;
-      L.mean[j] = make_float2(3.0e38f, 3.0e38f);
-      L.cov[j] = make_float4(1.0f, 0.0f, 0.0f, 1.0f);
-      L.alpha[j] = 0.0f;
+      const float *c = a.cov2d + 4 * (int64_t)id;
+      mm = make_float2(m[0], m[1]);
+      cv = make_float4(c[0], c[1], c[2], c[3]);
+      al = fminf(a.alpha[id], 0.99f);
+      bool drop;
+      box = skip_box(cv, mm, al, drop);
+      keep = !drop && !(mm.x + box.x < tx0) && !(mm.x - box.x > tx1) && !(mm.y + box.y < ty0) &&
+             !(mm.y - box.y > ty1);
     }
+    // ids outside [0, n) are dropped: no reads of the caller's arrays
+  }
+  const unsigned ballot = __ballot_sync(kFull, keep);
+  if (lane == 0) s_wcount[warp] = __popc(ballot);
+  __syncthreads();
+  int before = 0, total = 0;
+  for (int w = 0; w < nwarps; ++w) {
+    const int c = s_wcount[w];
+    before += (w < warp) ? c : 0;
+    total += c;
+  }
+  if (keep) {
+    const int pos = before + __popc(ballot & lanemask_lt());
+    L.ids[pos] = id;
+    L.mean[pos] = mm;
+    L.cov[pos] = cv;
+    L.alpha[pos] = al;
+    L.box[pos] = box;
   }
   __syncthreads();
-  const int total = nb * 3 * CC;
-  for (int f = t; f < total; f += nthr) {
+  const int count = total * 3 * CC;
+  for (int f = t; f < count; f += nthr) {
     int j = f / (3 * CC);
     int rem = f - j * (3 * CC);
     int ch = rem / CC;
     int k = rem - ch * CC;
-    const int id = L.ids[j];
-    L.sh[j * GSH + ch * CCP + k] = id >= 0 ? a.sh[((int64_t)id * 3 + ch) * a.sh_stride + k] : 0.0f;
+    L.sh[j * GSH + ch * CCP + k] = a.sh[((int64_t)L.ids[j] * 3 + ch) * a.sh_stride + k];
   }
   __syncthreads();
+  return total;
+}
+
+template <int C>
+__device__ __forceinline__ void pack_basis(const float *Y, float2 *Y2) {
+  constexpr int CC = Sh<C>::CC;
+#pragma unroll
+  for (int j = 0; j < Sh<C>::NY2; ++j)
+    Y2[j] = make_float2(Y[2 * j], 2 * j + 1 < CC ? Y[(2 * j + 1) < CC ? 2 * j + 1 : 0] : 0.0f);
 }
 
 template <int C, int MAXT>
 __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a) {
-  constexpr int CC = Sh<C>::CC, GSH = Sh<C>::GSH;
+  constexpr int GSH = Sh<C>::GSH, CCP = Sh<C>::CCP;
   extern __shared__ float4 smem4[];
+  __shared__ int s_wcount[32];
   const int nthr = blockDim.x;
-  const int B = nthr;
+  const int B = a.batch;
   SmemLayout L = carve<C>(reinterpret_cast<float *>(smem4), B);
 
   const int tile = blockIdx.x;
   const int t = threadIdx.x;
-  const int gx = (tile % a.n_tiles_w) * a.tile_w + t % a.tile_w;
-  const int gy = (tile / a.n_tiles_w) * a.tile_h + t / a.tile_w;
+  int gx, gy;
+  pixel_of(a, tile, t, gx, gy);
   const bool inside = t < a.tile_w * a.tile_h && gx < a.width && gy < a.height;
   const int s0 = a.start[tile];
   const int n = tile_list_length(a, tile, s0);
@@ -197,24 +319,34 @@ __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a
   }
   const float px = fmaf((float)gx, a.psx, a.topleft[0]);
   const float py = fmaf((float)gy, a.psy, a.topleft[1]);
-  float Y[CC];
-  sh_basis<C>(a.c2w, px, py, Y);
+  float2 Y2[Sh<C>::NY2];
+  {
+    float Y[Sh<C>::CC];
+    sh_basis<C>(a.c2w, px, py, Y);
+    pack_basis<C>(Y, Y2);
+  }
   float o0 = 0.0f, o1 = 0.0f, o2 = 0.0f, T = 1.0f;
   const float thr = a.T_thresh;
   bool done = !inside;
+  float tx0, tx1, ty0, ty1;
+  tile_bounds(a, tile, tx0, tx1, ty0, ty1);
 
   for (int base = 0; base < n; base += B) {
     if (__syncthreads_and(done)) break;
     const int nb = min(B, n - base);
-    load_batch<C>(a, L, s0 + base, nb, t, nthr);
+    const int nk = load_batch<C>(a, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1, s_wcount);
     if (!done) {
-      for (int i = 0; i < nb; ++i) {
+      for (int i = 0; i < nk; ++i) {
         if (T < thr) {
           done = true;
           break;
         }
+        const float2 m = L.mean[i];
+        const float2 h = L.box[i];
+        const float x = px - m.x, y = py - m.y;
+        if (fabsf(x) > h.x || fabsf(y) > h.y) continue;
         const float al = L.alpha[i];
-        const float radial = radial_of(L.cov[i], L.mean[i], px, py);
+        const float radial = radial_of(L.cov[i], x, y);
         if (surely_skipped(radial, al)) continue;
         const float G = gsx_expf(-0.5f * radial);
         float coeff = al * T;
@@ -222,9 +354,9 @@ __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a
         if (al * G < kMinRenderAlpha) continue;
         if (isnan(coeff)) coeff = 0.0f;
         const float *s = L.sh + i * GSH;
-        float y0 = gsx_sigmoidf(sh_dot<C>(s, Y));
-        float y1 = gsx_sigmoidf(sh_dot<C>(s + Sh<C>::CCP, Y));
-        float y2 = gsx_sigmoidf(sh_dot<C>(s + 2 * Sh<C>::CCP, Y));
+        float y0 = fast_sigmoid(sh_logit<C>(s, Y2));
+        float y1 = fast_sigmoid(sh_logit<C>(s + CCP, Y2));
+        float y2 = fast_sigmoid(sh_logit<C>(s + 2 * CCP, Y2));
         if (isnan(y0 * coeff)) y0 = 0.0f;
         if (isnan(y1 * coeff)) y1 = 0.0f;
         if (isnan(y2 * coeff)) y2 = 0.0f;
@@ -244,49 +376,129 @@ __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a
   }
 }
 
-// Butterfly reduce-scatter of V = 32*R values over a warp: afterwards lane l
-// holds the warp sums of value indices l*R .. l*R + R - 1 in v[0..R-1].
-template <int V>
-__device__ __forceinline__ void warp_reduce_scatter(float (&v)[V], int lane) {
+// Sum of six per-lane values over the warp: reduce-scatter over offsets 16,
+// 8, 4 (eight slots, two spare), then a butterfly over 2 and 1.  Afterwards
+// lanes 4j hold the warp sum of value j.
+__device__ __forceinline__ float warp_sum6(const float (&sc)[6], int lane) {
+  float v[8] = {sc[0], sc[1], sc[2], sc[3], sc[4], sc[5], 0.0f, 0.0f};
 #pragma unroll
-  for (int s = 0; s < 5; ++s) {
+  for (int s = 0; s < 3; ++s) {
     const int o = 16 >> s;
-    const int half = (V >> s) / 2;
+    const int half = 4 >> s;
     const bool up = (lane & o) != 0;
 #pragma unroll
     for (int k = 0; k < half; ++k) {
-      float send = up ? v[k] : v[k + half];
-      float keep = up ? v[k + half] : v[k];
+      const float send = up ? v[k] : v[k + half];
+      const float keep = up ? v[k + half] : v[k];
       v[k] = keep + __shfl_xor_sync(kFull, send, o);
     }
   }
+  float r = v[0];
+  r += __shfl_xor_sync(kFull, r, 2);
+  r += __shfl_xor_sync(kFull, r, 1);
+  return r;
+}
+
+__device__ __forceinline__ void split_tf32(float x, uint32_t &hi, uint32_t &lo) {
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hi) : "f"(x));
+  const float rest = x - __uint_as_float(hi);
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lo) : "f"(rest));
+}
+
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
+                                         uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+constexpr int kSlots = 5;     // Gaussians per warp matrix product (15 of 16 rows)
+constexpr int kWStride = 36;  // row stride of the 16 x 32 weight matrix (bank-conflict free)
+constexpr int kYStride = 24;  // row stride of the 32 x 16 basis matrix (bank-conflict free)
+
+// SH gradients of the staged Gaussians: D[r][k] = sum_p W[r][p] * Y[p][k] for
+// rows r = 3*slot + channel, added into the batch accumulators.
+template <int C>
+__device__ __forceinline__ void flush_sh_group(const float *Ws, const float *Ys, const int *slots,
+                                               int nslot, float *s_grad, int lane) {
+  constexpr int CC = Sh<C>::CC;
+  constexpr int NT = (CC + 7) / 8;
+  constexpr int NV = 6 + 3 * CC;
+  const int g = lane >> 2, tq = lane & 3;
+  float d[NT][4];
+#pragma unroll
+  for (int nt = 0; nt < NT; ++nt) d[nt][0] = d[nt][1] = d[nt][2] = d[nt][3] = 0.0f;
+#pragma unroll
+  for (int ks = 0; ks < 4; ++ks) {
+    uint32_t ah[4], al[4];
+    split_tf32(Ws[g * kWStride + 8 * ks + tq], ah[0], al[0]);
+    split_tf32(Ws[(g + 8) * kWStride + 8 * ks + tq], ah[1], al[1]);
+    split_tf32(Ws[g * kWStride + 8 * ks + tq + 4], ah[2], al[2]);
+    split_tf32(Ws[(g + 8) * kWStride + 8 * ks + tq + 4], ah[3], al[3]);
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) {
+      uint32_t b0h, b0l, b1h, b1l;
+      split_tf32(Ys[(8 * ks + tq) * kYStride + 8 * nt + g], b0h, b0l);
+      split_tf32(Ys[(8 * ks + tq + 4) * kYStride + 8 * nt + g], b1h, b1l);
+      mma_tf32(d[nt], ah, b0h, b1h);
+      mma_tf32(d[nt], ah, b0l, b1l);
+      mma_tf32(d[nt], al, b0h, b1h);
+    }
+  }
+  const int rows = 3 * nslot;
+#pragma unroll
+  for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int r = g + ((e & 2) ? 8 : 0);
+      const int k = 8 * nt + 2 * tq + (e & 1);
+      if (r < rows && k < CC && d[nt][e] != 0.0f) {
+        const int slot = r / 3, ch = r - 3 * slot;
+        atomicAdd(&s_grad[slots[slot] * NV + 6 + ch * CC + k], d[nt][e]);
+      }
+    }
 }
 
 template <int C, int MAXT>
-__global__ void __launch_bounds__(MAXT) raster_backward_kernel(const RasterArgs a, int B) {
+__global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1)
+    raster_backward_kernel(const RasterArgs a) {
   constexpr int CC = Sh<C>::CC, CCP = Sh<C>::CCP, GSH = Sh<C>::GSH;
   constexpr int NV = 6 + 3 * CC;  // gm0 gm1 gc0 gc12 gc3 galpha gsh[3*CC]
-  constexpr int V = ((NV + 31) / 32) * 32;
-  constexpr int R = V / 32;
   extern __shared__ float4 smem4[];
+  __shared__ int s_wcount[32];
   float *smem = reinterpret_cast<float *>(smem4);
+  const int B = a.batch;
+  const int nthr = blockDim.x, nwarps = nthr >> 5;
   SmemLayout L = carve<C>(smem, B);
-  float *s_grad = L.sh + B * GSH;               // [B][NV]
-  int *s_touched = reinterpret_cast<int *>(s_grad + B * NV);
+  float *s_grad = L.sh + B * GSH;                                         // [B][NV]
+  float *s_w = s_grad + B * NV;                                           // [nwarps][16][kWStride]
+  float *s_y = s_w + nwarps * 16 * kWStride;                              // [nwarps][32][kYStride]
+  int *s_slots = reinterpret_cast<int *>(s_y + nwarps * 32 * kYStride);  // [nwarps][8]
+  int *s_touched = s_slots + nwarps * 8;                                  // [B]
 
-  const int nthr = blockDim.x;
   const int tile = blockIdx.x;
-  const int t = threadIdx.x, lane = t & 31;
-  const int gx = (tile % a.n_tiles_w) * a.tile_w + t % a.tile_w;
-  const int gy = (tile / a.n_tiles_w) * a.tile_h + t / a.tile_w;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  int gx, gy;
+  pixel_of(a, tile, t, gx, gy);
   const bool inside = t < a.tile_w * a.tile_h && gx < a.width && gy < a.height;
   const int s0 = a.start[tile];
   const int n = tile_list_length(a, tile, s0);
   if (n <= 0) return;
   const float px = fmaf((float)gx, a.psx, a.topleft[0]);
   const float py = fmaf((float)gy, a.psy, a.topleft[1]);
-  float Y[CC];
-  sh_basis<C>(a.c2w, px, py, Y);
+  float2 Y2[Sh<C>::NY2];
+  float *Ws = s_w + warp * 16 * kWStride;
+  float *Ys = s_y + warp * 32 * kYStride;
+  int *slots = s_slots + warp * 8;
+  {
+    float Y[CC];
+    sh_basis<C>(a.c2w, px, py, Y);
+    pack_basis<C>(Y, Y2);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) Ys[lane * kYStride + k] = k < CC ? Y[k < CC ? k : 0] : 0.0f;
+  }
   float fin[3] = {0.0f, 0.0f, 0.0f}, go[3] = {0.0f, 0.0f, 0.0f};
   if (inside) {
     const int64_t pix = 3 * ((int64_t)gy * a.width + gx);
@@ -300,20 +512,22 @@ __global__ void __launch_bounds__(MAXT) raster_backward_kernel(const RasterArgs 
   float T = 1.0f;
   const float thr = a.T_thresh;
   bool done = !inside;
+  float tx0, tx1, ty0, ty1;
+  tile_bounds(a, tile, tx0, tx1, ty0, ty1);
 
   for (int base = 0; base < n; base += B) {
     if (__syncthreads_and(done)) break;
     const int nb = min(B, n - base);
     for (int f = t; f < nb * NV; f += nthr) s_grad[f] = 0.0f;
     for (int j = t; j < nb; j += nthr) s_touched[j] = 0;
-    load_batch<C>(a, L, s0 + base, nb, t, nthr);
+    const int nk = load_batch<C>(a, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1, s_wcount);
 
-    for (int i = 0; i < nb; ++i) {
+    int nslot = 0;  // warp-uniform: Gaussians staged in this warp's weight matrix
+    for (int i = 0; i < nk; ++i) {
       if (__all_sync(kFull, done)) break;
       bool contrib = false;
-      float v[V];
-#pragma unroll
-      for (int k = 0; k < V; ++k) v[k] = 0.0f;
+      float sc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+      float w[3] = {0.0f, 0.0f, 0.0f};
       if (!done) {
         if (T < thr) {
           done = true;
@@ -321,8 +535,11 @@ __global__ void __launch_bounds__(MAXT) raster_backward_kernel(const RasterArgs 
           const float al = L.alpha[i];
           const float4 cv = L.cov[i];
           const float2 m = L.mean[i];
-          const float radial = radial_of(cv, m, px, py);
-          if (!surely_skipped(radial, al)) {
+          const float2 h = L.box[i];
+          const float x = px - m.x, yy = py - m.y;
+          const bool outside = fabsf(x) > h.x || fabsf(yy) > h.y;
+          const float radial = outside ? 0.0f : radial_of(cv, x, yy);
+          if (!outside && !surely_skipped(radial, al)) {
             const float G = gsx_expf(-0.5f * radial);
             if (!(al * G < kMinRenderAlpha)) {
               contrib = true;
@@ -332,55 +549,64 @@ __global__ void __launch_bounds__(MAXT) raster_backward_kernel(const RasterArgs 
               float y[3];
 #pragma unroll
               for (int ch = 0; ch < 3; ++ch) {
-                y[ch] = gsx_sigmoidf(sh_dot<C>(s + ch * CCP, Y));
+                y[ch] = fast_sigmoid(sh_logit<C>(s + ch * CCP, Y2));
                 if (isnan(y[ch] * coeff)) y[ch] = 0.0f;
                 o[ch] = fmaf(coeff, y[ch], o[ch]);
               }
 #pragma unroll
-              for (int ch = 0; ch < 3; ++ch) {
-                const float w = coeff * (y[ch] * (1.0f - y[ch])) * go[ch];
-#pragma unroll
-                for (int k = 0; k < CC; ++k) v[6 + ch * CC + k] = w * Y[k];
-              }
+              for (int ch = 0; ch < 3; ++ch) w[ch] = coeff * (y[ch] * (1.0f - y[ch])) * go[ch];
               const float one_m = fmaf(-al, G, 1.0f);
+              const float inv_one_m = 1.0f / one_m;
               float P = 0.0f;
 #pragma unroll
               for (int ch = 0; ch < 3; ++ch) {
-                const float q = (fin[ch] - o[ch]) / one_m;
+                const float q = (fin[ch] - o[ch]) * inv_one_m;
                 P = fmaf(go[ch], fmaf(y[ch], T, -q), P);
               }
               const float dg = P * al * G;
-              const float det = fmaf(cv.x, cv.w, -(cv.y * cv.z));
-              const float x = px - m.x, yy = py - m.y;
-              const float tmpx = fmaf(x, cv.w, -(yy * cv.z)) / det;
-              const float tmpy = fmaf(-x, cv.y, yy * cv.x) / det;
+              const float inv_det = 1.0f / fmaf(cv.x, cv.w, -(cv.y * cv.z));
+              const float tmpx = fmaf(x, cv.w, -(yy * cv.z)) * inv_det;
+              const float tmpy = fmaf(-x, cv.y, yy * cv.x) * inv_det;
               const float dx = dg * tmpx, dy = dg * tmpy;
-              v[0] = dx;
-              v[1] = dy;
-              v[2] = 0.5f * (dx * tmpx);
-              v[3] = 0.5f * (dx * tmpy);
-              v[4] = 0.5f * (dy * tmpy);
-              v[5] = P * G;
+              sc[0] = dx;
+              sc[1] = dy;
+              sc[2] = 0.5f * (dx * tmpx);
+              sc[3] = 0.5f * (dx * tmpy);
+              sc[4] = 0.5f * (dy * tmpy);
+              sc[5] = P * G;
               T = T * one_m;
             }
           }
         }
       }
       if (__ballot_sync(kFull, contrib)) {
-        warp_reduce_scatter<V>(v, lane);
+        const float r = warp_sum6(sc, lane);
+        if ((lane & 3) == 0 && (lane >> 2) < 6 && r != 0.0f)
+          atomicAdd(&s_grad[i * NV + (lane >> 2)], r);
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-          const int idx = lane * R + r;
-          if (idx < NV && v[r] != 0.0f) atomicAdd(&s_grad[i * NV + idx], v[r]);
+        for (int ch = 0; ch < 3; ++ch) Ws[(3 * nslot + ch) * kWStride + lane] = w[ch];
+        if (lane == 0) {
+          slots[nslot] = i;
+          s_touched[i] = 1;
         }
-        if (lane == 0) s_touched[i] = 1;
+        if (++nslot == kSlots) {
+          __syncwarp();
+          flush_sh_group<C>(Ws, Ys, slots, nslot, s_grad, lane);
+          __syncwarp();
+          nslot = 0;
+        }
       }
+    }
+    if (nslot > 0) {
+      __syncwarp();
+      flush_sh_group<C>(Ws, Ys, slots, nslot, s_grad, lane);
+      __syncwarp();
     }
     if (!done && T < thr) done = true;
     __syncthreads();
-    for (int f = t; f < nb * NV; f += nthr) {
+    for (int f = t; f < nk * NV; f += nthr) {
       const int j = f / NV, idx = f - j * NV;
-      if (!s_touched[j] || L.ids[j] < 0) continue;
+      if (!s_touched[j]) continue;
       const float val = s_grad[f];
       if (val == 0.0f) continue;
       const int64_t id = L.ids[j];
@@ -404,27 +630,30 @@ __global__ void __launch_bounds__(MAXT) raster_backward_kernel(const RasterArgs 
 }
 
 template <int C>
-size_t fwd_smem(int nthr) {
-  return (size_t)nthr * (8 + Sh<C>::GSH) * sizeof(float);
+size_t fwd_smem(int B) {
+  return (size_t)B * (10 + Sh<C>::GSH) * sizeof(float);
 }
 
 template <int C>
-size_t bwd_smem(int B) {
+size_t bwd_smem(int B, int nthr) {
   constexpr int NV = 6 + 3 * Sh<C>::CC;
-  return (size_t)B * (8 + Sh<C>::GSH + NV + 1) * sizeof(float);
+  const int nwarps = nthr / 32;
+  return (size_t)B * (10 + Sh<C>::GSH + NV + 1) * sizeof(float) +
+         (size_t)nwarps * (16 * kWStride + 32 * kYStride + 8) * sizeof(float);
 }
 
 inline int block_threads(const RasterArgs &a) { return (a.tile_w * a.tile_h + 31) / 32 * 32; }
 
 template <int C, int MAXT>
-int launch_fwd_tt(const RasterArgs &a, cudaStream_t s) {
+int launch_fwd_tt(RasterArgs a, cudaStream_t s) {
   const int nthr = block_threads(a);
-  const size_t smem = fwd_smem<C>(nthr);
+  a.batch = nthr < 128 ? nthr : 128;
+  const size_t smem = fwd_smem<C>(a.batch);
   cudaError_t e = cudaFuncSetAttribute(raster_forward_kernel<C, MAXT>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_status(e, "raster_forward smem attribute");
   const unsigned grid = (unsigned)(a.n_tiles_w * a.n_tiles_h);
+  count_launches(1);
   raster_forward_kernel<C, MAXT><<<grid, nthr, smem, s>>>(a);
   return cuda_status(cudaGetLastError(), "raster_forward_kernel launch");
 }
@@ -435,16 +664,16 @@ int launch_fwd_t(const RasterArgs &a, cudaStream_t s) {
 }
 
 template <int C, int MAXT>
-int launch_bwd_tt(const RasterArgs &a, cudaStream_t s) {
+int launch_bwd_tt(RasterArgs a, cudaStream_t s) {
   const int nthr = block_threads(a);
-  const int B = nthr < 128 ? nthr : 128;
-  const size_t smem = bwd_smem<C>(B);
+  a.batch = nthr < 64 ? nthr : 64;
+  const size_t smem = bwd_smem<C>(a.batch, nthr);
   cudaError_t e = cudaFuncSetAttribute(raster_backward_kernel<C, MAXT>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_status(e, "raster_backward smem attribute");
   const unsigned grid = (unsigned)(a.n_tiles_w * a.n_tiles_h);
-  raster_backward_kernel<C, MAXT><<<grid, nthr, smem, s>>>(a, B);
+  count_launches(1);
+  raster_backward_kernel<C, MAXT><<<grid, nthr, smem, s>>>(a);
   return cuda_status(cudaGetLastError(), "raster_backward_kernel launch");
 }
 

@@ -43,6 +43,8 @@ const char *gsx_status_string(int status);
 const char *gsx_last_error(void);
 /* ABI version of this library (increments on any signature change). */
 int gsx_abi_version(void);
+/* Number of kernels this library has launched in this process so far. */
+uint64_t gsx_kernel_launch_count(void);
 
 /* ---- 1. reference `_gs` hot-path entry points --------------------------- */
 

@@ -1,10 +1,12 @@
 """CUDA path vs the CPU oracle on the same seeded inputs.
 
 Tolerances (FP32):
-  * projection, binning, forward image: bit-exact.  The kernels and the
-    oracle follow one operation sequence (explicit fmaf, IEEE division and
-    sqrt, the shared exp), so every cull / skip / stop / truncation decision
-    and every pixel agrees exactly;
+  * projection and binning: bit-exact.  The kernels and the oracle follow one
+    operation sequence (explicit fmaf, IEEE division and sqrt, the shared
+    exp), so every cull / skip / stop / truncation decision agrees exactly;
+  * forward image: max-abs 2e-6.  The decisions above are exact; only the
+    colour arithmetic (paired-FMA SH dot products, hardware ex2/rcp sigmoid)
+    differs from the oracle's, by a few ulp;
   * gradients: max |cuda - oracle| <= 1e-4 * max |oracle| per tensor -- the
     oracle sums in double and in tile order, the GPU in float through warp
     reductions and atomics, so only summation rounding differs.
@@ -21,6 +23,14 @@ from oracle import oracle as O  # noqa: E402
 pytestmark = pytest.mark.gpu
 
 GRAD_REL = 1e-4
+IMG_ATOL = 2e-6
+
+
+def assert_image_close(got, ref):
+    d = np.abs(np.asarray(got, np.float64) - np.asarray(ref, np.float64))
+    assert d.max(initial=0.0) <= IMG_ATOL, f"image max |d| = {d.max():.3g}"
+    # a pixel the oracle leaves black (no contribution) must stay exactly black
+    assert np.all(np.asarray(got)[np.asarray(ref) == 0] == 0)
 
 
 def dev():
@@ -111,7 +121,7 @@ def test_fused_pipeline_matches_oracle(name):
     wl = WORKLOADS[name]()
     ref = oracle_view(wl)
     got = gpu_pipeline(wl)
-    np.testing.assert_array_equal(got["image"], ref["image"])
+    assert_image_close(got["image"], ref["image"])
     for k, g in got["grads"].items():
         e = rel_err(g, ref["param_grads"][k])
         assert e <= GRAD_REL, f"{k}: relative max error {e:.3g}"
@@ -137,7 +147,7 @@ def test_tile_shapes(tile):
     psx, psy = np.float32(1 / cam.fx), np.float32(1 / cam.fy)
     img = O.render_fwd(P, pr["mean2d"], pr["cov2d"], sc.sh, pr["alpha"], b["start"], b["end"], b["ids"], tl,
                        view.c2w, psx, psy)
-    np.testing.assert_array_equal(got["image"], img)
+    assert_image_close(got["image"], img)
 
 
 def test_dropin_gs_functions_match_oracle():
@@ -181,7 +191,7 @@ def test_dropin_gs_functions_match_oracle():
     P = O.raster_params(cam.w, cam.h, 16, 16, C)
     psx, psy = np.float32(1 / cam.fx), np.float32(1 / cam.fy)
     img = O.render_fwd(P, mean2d, cov2d, sh, alpha, b["start"], b["end"], b["ids"], topleft, view.c2w, psx, psy)
-    np.testing.assert_array_equal(out.detach().cpu().numpy().reshape(cam.h, cam.w, 3), img)
+    assert_image_close(out.detach().cpu().numpy().reshape(cam.h, cam.w, 3), img)
     (out * t(wl.grad_weight.reshape(-1))).sum().backward()
     g = O.render_bwd(P, mean2d, cov2d, sh, alpha, b["start"], b["end"], b["ids"], topleft, view.c2w, psx, psy,
                      img, wl.grad_weight)
@@ -201,7 +211,7 @@ def test_equal_depth_ties_in_index_order():
     wl = S.Workload("ties", sc, base.views, base.grad_weight)
     ref = oracle_view(wl)
     got = gpu_pipeline(wl)
-    np.testing.assert_array_equal(got["image"], ref["image"])
+    assert_image_close(got["image"], ref["image"])
     ids = ref["bins"]["ids"]
     s, e = ref["bins"]["start"], ref["bins"]["end"]
     for tile in np.nonzero(s >= 0)[0]:
@@ -224,7 +234,7 @@ def test_big_gaussians_many_tiles():
     ref = oracle_view(wl)
     assert ref["bins"]["K"] > 300 * 20
     got = gpu_pipeline(wl)
-    np.testing.assert_array_equal(got["image"], ref["image"])
+    assert_image_close(got["image"], ref["image"])
     for k, g in got["grads"].items():
         assert rel_err(g, ref["param_grads"][k]) <= GRAD_REL, k
 
@@ -261,7 +271,7 @@ def test_sh_order_below_stored_coefficients():
     got = gpu_pipeline(wl, st)
     sliced = S.Scene(sc.mean, sc.qvec, sc.log_scale, np.ascontiguousarray(sc.sh[..., :4]), sc.alpha_logit, 2)
     ref = O.render_view(sliced, wl.views[0], wl.grad_weight)
-    np.testing.assert_array_equal(got["image"], ref["image"])
+    assert_image_close(got["image"], ref["image"])
     g = got["grads"]["sh"]
     assert np.all(g[..., 4:] == 0)
     assert rel_err(g[..., :4], ref["param_grads"]["sh"]) <= GRAD_REL
