@@ -100,6 +100,11 @@ SIGNATURES = {
         c_int,
         [c_int64, P, P, P, c_int32, c_int32, c_int64, P, P, P, POINTER(c_int64), P, c_size_t, P],
     ),
+    "gsx_bin_gaussians_async": (
+        c_int,
+        [c_int64, P, P, P, c_int32, c_int32, c_int64, P, P, P, P, c_size_t, P],
+    ),
+    "gsx_binning_status": (c_int, [P, c_int64, c_int64, c_int32, c_int32, POINTER(c_int64), P]),
     "gsx_render_forward": (
         c_int,
         [POINTER(GsxRasterParams), c_int64, c_int64, P, P, P, P, P, P, P, P, P, P, P],

@@ -135,6 +135,32 @@ int gsx_bin_gaussians(int64_t n, const int32_t *rect, const int32_t *counts,
                      as_stream(stream));
 }
 
+int gsx_bin_gaussians_async(int64_t n, const int32_t *rect, const int32_t *counts,
+                            const float *depth, int32_t n_tiles_w, int32_t n_tiles_h,
+                            int64_t key_capacity, int32_t *gaussian_ids, int32_t *start,
+                            int32_t *end, void *workspace, size_t workspace_bytes,
+                            void *stream) {
+  g_err[0] = 0;
+  int st = check_binning_sizes(n, key_capacity, n_tiles_h, n_tiles_w);
+  if (st != GSX_OK) return st;
+  GSX_REQUIRE(start && end, "null output pointer");
+  GSX_REQUIRE(n == 0 || (rect && counts && depth), "null input pointer");
+  GSX_REQUIRE(key_capacity == 0 || gaussian_ids, "null gaussian_ids");
+  return run_binning_async(n, rect, rect + 2, 4, counts, depth, n_tiles_w, n_tiles_h,
+                           key_capacity, gaussian_ids, start, end, workspace, workspace_bytes,
+                           as_stream(stream));
+}
+
+int gsx_binning_status(const void *workspace, int64_t n_gaussians, int64_t key_capacity,
+                       int32_t n_tiles_w, int32_t n_tiles_h, int64_t *n_keys_out,
+                       void *stream) {
+  g_err[0] = 0;
+  GSX_REQUIRE(workspace, "null workspace");
+  GSX_REQUIRE(n_gaussians >= 0 && key_capacity >= 0, "negative size");
+  return binning_status(workspace, n_gaussians, key_capacity, n_tiles_w, n_tiles_h, n_keys_out,
+                        nullptr, as_stream(stream));
+}
+
 static int check_raster(const RasterArgs &a, int C, int64_t n, int64_t n_keys) {
   GSX_REQUIRE(C >= 1 && C <= 4, "SH order C must be 1..4 (got %d)", C);
   GSX_REQUIRE(a.tile_w > 0 && a.tile_h > 0 && a.tile_w * a.tile_h <= 1024,

@@ -93,9 +93,11 @@ __device__ __forceinline__ T block_exclusive_scan(T v, T *s_tmp, T *total) {
 
 // Histogram of `passes` 8-bit digits (starting at bit 0) of n keys.
 __global__ void __launch_bounds__(kThreads)
-    histogram_kernel(const uint32_t *__restrict__ keys, uint32_t n, int passes,
+    histogram_kernel(const uint32_t *__restrict__ keys, uint32_t n_max,
+                     const uint32_t *__restrict__ n_dev, int passes,
                      uint32_t *__restrict__ hist) {
   __shared__ uint32_t sh[4 * 256];
+  const uint32_t n = n_dev ? min(*n_dev, n_max) : n_max;
   for (int i = threadIdx.x; i < 4 * 256; i += kThreads) sh[i] = 0;
   __syncthreads();
   for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
@@ -108,13 +110,17 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // One stable LSD pass on the 8-bit digit at `shift`.  vals_in == nullptr
-// means value = input position.
+// means value = input position.  The item count is n_max, or *n_dev when
+// given (a count produced on the device); chunks past it exit at once, and
+// no chunk ever waits on a later one.
 __global__ void __launch_bounds__(kThreads)
     onesweep_kernel(const uint32_t *__restrict__ keys_in,
                     const uint32_t *__restrict__ vals_in, uint32_t *__restrict__ keys_out,
-                    uint32_t *__restrict__ vals_out, uint32_t n, int shift,
+                    uint32_t *__restrict__ vals_out, uint32_t n_max,
+                    const uint32_t *__restrict__ n_dev, int shift,
                     const uint32_t *__restrict__ pass_hist, uint32_t *status,
                     uint32_t *chunk_counter, uint32_t *error) {
+  const uint32_t n = n_dev ? min(*n_dev, n_max) : n_max;
   __shared__ uint32_t s_warp[kWarps][256];
   __shared__ uint32_t s_cta_excl[256];
   __shared__ uint32_t s_glob[256];
@@ -129,6 +135,7 @@ __global__ void __launch_bounds__(kThreads)
   __syncthreads();
   const uint32_t chunk = s_chunk;
   const uint32_t base = chunk * (uint32_t)kTile;
+  if (base >= n) return;  // block-uniform
   const uint32_t lt = lanemask_lt();
 
   uint32_t keys[kItems], vals[kItems], rank[kItems];
@@ -234,7 +241,8 @@ __global__ void __launch_bounds__(kThreads)
                 int rect_stride, const int32_t *__restrict__ counts, int32_t n_tiles_w,
                 int32_t n_tiles_h, uint32_t *__restrict__ tile_out, uint32_t *__restrict__ id_out,
                 unsigned long long capacity, unsigned long long *status,
-                uint32_t *chunk_counter, unsigned long long *total_out, uint32_t *error) {
+                uint32_t *chunk_counter, unsigned long long *total_out, uint32_t *k_eff,
+                uint32_t *error) {
   __shared__ unsigned long long s_tmp[kWarps];
   __shared__ unsigned long long s_prefix;
   __shared__ uint32_t s_chunk;
@@ -295,7 +303,11 @@ __global__ void __launch_bounds__(kThreads)
       st_volatile64(mine, kFlag64Prefix | (prev + block_total));
     }
     s_prefix = prev;
-    if ((unsigned long long)(chunk + 1) * kEmitTile >= n) *total_out = prev + block_total;
+    if ((unsigned long long)(chunk + 1) * kEmitTile >= n) {
+      const unsigned long long total = prev + block_total;
+      *total_out = total;
+      *k_eff = (uint32_t)(total < capacity ? total : capacity);
+    }
   }
   __syncthreads();
   unsigned long long off = s_prefix + excl;
@@ -322,8 +334,10 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-__global__ void ranges_kernel(const uint32_t *__restrict__ tiles, uint32_t K, uint32_t n_tiles,
-                              int32_t *__restrict__ start, int32_t *__restrict__ end) {
+__global__ void ranges_kernel(const uint32_t *__restrict__ tiles, const uint32_t *__restrict__ K_dev,
+                              uint32_t n_tiles, int32_t *__restrict__ start,
+                              int32_t *__restrict__ end) {
+  const uint32_t K = *K_dev;
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= K) return;
   const uint32_t t = tiles[i];
@@ -343,6 +357,7 @@ struct Workspace {
   uint32_t *counters;  // [16]
   uint32_t *error;
   unsigned long long *total;
+  uint32_t *k_eff;  // min(total, capacity), the key count the tile sort uses
   size_t status_words, emit_words;
   size_t bytes;
 };
@@ -370,27 +385,29 @@ Workspace carve_ws(void *base, int64_t n, int64_t cap) {
   w.counters = reinterpret_cast<uint32_t *>(take(16 * 4));
   w.error = reinterpret_cast<uint32_t *>(take(4));
   w.total = reinterpret_cast<unsigned long long *>(take(8));
+  w.k_eff = reinterpret_cast<uint32_t *>(take(4));
   w.bytes = off;
   return w;
 }
 
-// Stable LSD sort of n (key, value) pairs over `bits` low key bits.  The
-// final pass writes into (final_keys, final_vals); intermediate passes use
-// the two scratch buffers.  keys_in/vals_in are never written.
-int radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t n, int bits,
-               uint32_t *scratch_k[2], uint32_t *scratch_v[2], uint32_t *final_keys,
-               uint32_t *final_vals, const Workspace &w, cudaStream_t s) {
+// Stable LSD sort of n (key, value) pairs over `bits` low key bits; the count
+// is n_max, or *n_dev (at most n_max) when n_dev is given.  The final pass
+// writes into (final_keys, final_vals); intermediate passes use the two
+// scratch buffers.  keys_in/vals_in are never written.
+int radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t n_max,
+               const uint32_t *n_dev, int bits, uint32_t *scratch_k[2], uint32_t *scratch_v[2],
+               uint32_t *final_keys, uint32_t *final_vals, const Workspace &w, cudaStream_t s) {
   const int passes = (bits + 7) / 8;
-  if (n == 0 || passes == 0) return GSX_OK;
+  if (n_max == 0 || passes == 0) return GSX_OK;
   cudaError_t e = cudaMemsetAsync(w.hist, 0, 8 * 256 * 4, s);
   if (e != cudaSuccess) return cuda_status(e, "memset histogram");
-  uint32_t hist_grid = (n + kThreads * 16 - 1) / (kThreads * 16);
+  uint32_t hist_grid = (n_max + kThreads * 16 - 1) / (kThreads * 16);
   if (hist_grid > 1024u) hist_grid = 1024u;
   count_launches(1);
-  histogram_kernel<<<hist_grid, kThreads, 0, s>>>(keys_in, n, passes, w.hist);
+  histogram_kernel<<<hist_grid, kThreads, 0, s>>>(keys_in, n_max, n_dev, passes, w.hist);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_status(e, "histogram_kernel launch");
-  const uint32_t chunks = (n + kTile - 1) / kTile;
+  const uint32_t chunks = (n_max + kTile - 1) / kTile;
   const uint32_t *ki = keys_in, *vi = vals_in;
   for (int p = 0; p < passes; ++p) {
     const bool last = p == passes - 1;
@@ -400,8 +417,9 @@ int radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t n, int
     if (e == cudaSuccess) e = cudaMemsetAsync(w.counters + p, 0, 4, s);
     if (e != cudaSuccess) return cuda_status(e, "memset look-back status");
     count_launches(1);
-  onesweep_kernel<<<chunks, kThreads, 0, s>>>(ki, vi, ko, vo, n, 8 * p, w.hist + 256 * p,
-                                                 w.status, w.counters + p, w.error);
+    onesweep_kernel<<<chunks, kThreads, 0, s>>>(ki, vi, ko, vo, n_max, n_dev, 8 * p,
+                                                 w.hist + 256 * p, w.status, w.counters + p,
+                                                 w.error);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e, "onesweep_kernel launch");
     ki = ko;
@@ -423,11 +441,13 @@ size_t binning_workspace_bytes(int64_t n, int64_t cap, int64_t n_tiles) {
   return carve_ws(nullptr, n, cap).bytes;
 }
 
-int run_binning(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
-                int32_t rect_stride, const int32_t *counts, const float *depth,
-                int32_t n_tiles_w, int32_t n_tiles_h, int64_t capacity, int32_t *ids,
-                int32_t *start, int32_t *end, int64_t *n_keys_host, void *ws,
-                size_t ws_bytes, cudaStream_t s) {
+// Enqueue the whole binning on `s` without synchronising.  Keys beyond
+// `capacity` are not written; the key total and the error bits stay in the
+// workspace for binning_status.
+int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
+                      int32_t rect_stride, const int32_t *counts, const float *depth,
+                      int32_t n_tiles_w, int32_t n_tiles_h, int64_t capacity, int32_t *ids,
+                      int32_t *start, int32_t *end, void *ws, size_t ws_bytes, cudaStream_t s) {
   const int64_t n_tiles = (int64_t)n_tiles_w * n_tiles_h;
   Workspace w = carve_ws(ws, n, capacity);
   if (ws_bytes < w.bytes) {
@@ -436,18 +456,16 @@ int run_binning(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
   }
   cudaError_t e = cudaMemsetAsync(start, 0xff, sizeof(int32_t) * (size_t)n_tiles, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(end, 0xff, sizeof(int32_t) * (size_t)n_tiles, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(w.counters, 0, 16 * 4 + 0, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.counters, 0, 16 * 4, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(w.error, 0, 4, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(w.total, 0, 8, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.k_eff, 0, 4, s);
   if (e != cudaSuccess) return cuda_status(e, "memset binning state");
-  if (n == 0) {
-    *n_keys_host = 0;
-    return GSX_OK;
-  }
+  if (n == 0) return GSX_OK;
   const uint32_t nn = (uint32_t)n;
   // 1. Gaussians sorted by depth bits (values = Gaussian index)
   uint32_t *sk[2] = {w.dkeys[0], w.dkeys[1]}, *sv[2] = {w.dvals[0], w.dvals[1]};
-  int st = radix_sort(reinterpret_cast<const uint32_t *>(depth), nullptr, nn, 32, sk, sv,
+  int st = radix_sort(reinterpret_cast<const uint32_t *>(depth), nullptr, nn, nullptr, 32, sk, sv,
                       w.dkeys[1], w.dvals[1], w, s);
   if (st != GSX_OK) return st;
   // 2. scan of counts + emission
@@ -458,19 +476,55 @@ int run_binning(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
   count_launches(1);
   emit_kernel<<<emit_chunks, kThreads, 0, s>>>(
       w.dvals[1], nn, rect_tl, rect_br, rect_stride, counts, n_tiles_w, n_tiles_h, w.tkeys[0],
-      w.tvals[0], (unsigned long long)capacity, w.emit_status, w.counters + 8, w.total,
+      w.tvals[0], (unsigned long long)capacity, w.emit_status, w.counters + 8, w.total, w.k_eff,
       w.error);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_status(e, "emit_kernel launch");
+  if (capacity == 0) return GSX_OK;
+  const uint32_t cap = (uint32_t)capacity;
+  // 3. stable sort by tile id over the device-side key count.  Pass p writes
+  // tkeys[1] for even p and tkeys[0] for odd p; the last pass writes the ids
+  // into the caller's buffer and its keys into whichever tile buffer is not
+  // its input.
+  const int tile_bits = bits_for((uint64_t)(n_tiles - 1));
+  uint32_t *ids_u = reinterpret_cast<uint32_t *>(ids);
+  uint32_t *final_keys = w.tkeys[0];
+  if (tile_bits == 0) {
+    e = cudaMemcpyAsync(ids_u, w.tvals[0], 4 * (size_t)cap, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return cuda_status(e, "copy ids");
+  } else {
+    const int passes = (tile_bits + 7) / 8;
+    uint32_t *tk[2] = {w.tkeys[1], w.tkeys[0]}, *tv[2] = {w.tvals[1], w.tvals[0]};
+    final_keys = (passes & 1) ? w.tkeys[1] : w.tkeys[0];
+    st = radix_sort(w.tkeys[0], w.tvals[0], cap, w.k_eff, tile_bits, tk, tv, final_keys, ids_u, w,
+                    s);
+    if (st != GSX_OK) return st;
+  }
+  // 4. start / end
+  count_launches(1);
+  ranges_kernel<<<(cap + 255) / 256, 256, 0, s>>>(final_keys, w.k_eff, (uint32_t)n_tiles, start,
+                                                   end);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_status(e, "ranges_kernel launch");
+  return GSX_OK;
+}
+
+// Read the key total and error bits left by run_binning_async (synchronises
+// `s`) and turn them into a status.
+int binning_status(const void *ws, int64_t n, int64_t capacity, int32_t n_tiles_w,
+                   int32_t n_tiles_h, int64_t *n_keys_host, uint32_t *flags_host,
+                   cudaStream_t s) {
+  Workspace w = carve_ws(const_cast<void *>(ws), n, capacity);
   unsigned long long total_h = 0;
   uint32_t err_h = 0;
-  e = cudaMemcpyAsync(&total_h, w.total, 8, cudaMemcpyDeviceToHost, s);
+  cudaError_t e = cudaMemcpyAsync(&total_h, w.total, 8, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(&err_h, w.error, 4, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return cuda_status(e, "read key count");
-  *n_keys_host = (int64_t)total_h;
+  if (e != cudaSuccess) return cuda_status(e, "read binning status");
+  if (n_keys_host) *n_keys_host = (int64_t)total_h;
+  if (flags_host) *flags_host = err_h;
   if (err_h & kErrTimeout) {
-    set_error("binning: a look-back wait expired (depth sort or key scan)");
+    set_error("binning: a look-back wait expired");
     return GSX_ERR_TIMEOUT;
   }
   if (err_h & kErrCount) {
@@ -489,37 +543,18 @@ int run_binning(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
     set_error("binning: %llu keys exceed the capacity of %lld", total_h, (long long)capacity);
     return GSX_ERR_CAPACITY;
   }
-  const uint32_t K = (uint32_t)total_h;
-  if (K == 0) return GSX_OK;
-  // 3. stable sort by tile id.  Pass p writes tkeys[1] for even p and
-  // tkeys[0] for odd p; the last pass writes the ids into the caller's buffer
-  // and its keys into whichever tile buffer is not its input.
-  const int tile_bits = bits_for((uint64_t)(n_tiles - 1));
-  uint32_t *ids_u = reinterpret_cast<uint32_t *>(ids);
-  uint32_t *final_keys = w.tkeys[0];
-  if (tile_bits == 0) {
-    e = cudaMemcpyAsync(ids_u, w.tvals[0], 4 * (size_t)K, cudaMemcpyDeviceToDevice, s);
-    if (e != cudaSuccess) return cuda_status(e, "copy ids");
-  } else {
-    const int passes = (tile_bits + 7) / 8;
-    uint32_t *tk[2] = {w.tkeys[1], w.tkeys[0]}, *tv[2] = {w.tvals[1], w.tvals[0]};
-    final_keys = (passes & 1) ? w.tkeys[1] : w.tkeys[0];
-    st = radix_sort(w.tkeys[0], w.tvals[0], K, tile_bits, tk, tv, final_keys, ids_u, w, s);
-    if (st != GSX_OK) return st;
-  }
-  // 4. start / end
-  count_launches(1);
-  ranges_kernel<<<(K + 255) / 256, 256, 0, s>>>(final_keys, K, (uint32_t)n_tiles, start, end);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_status(e, "ranges_kernel launch");
-  e = cudaMemcpyAsync(&err_h, w.error, 4, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return cuda_status(e, "read binning status");
-  if (err_h & kErrTimeout) {
-    set_error("binning: a look-back wait expired (tile sort)");
-    return GSX_ERR_TIMEOUT;
-  }
   return GSX_OK;
+}
+
+int run_binning(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
+                int32_t rect_stride, const int32_t *counts, const float *depth,
+                int32_t n_tiles_w, int32_t n_tiles_h, int64_t capacity, int32_t *ids,
+                int32_t *start, int32_t *end, int64_t *n_keys_host, void *ws,
+                size_t ws_bytes, cudaStream_t s) {
+  int st = run_binning_async(n, rect_tl, rect_br, rect_stride, counts, depth, n_tiles_w,
+                             n_tiles_h, capacity, ids, start, end, ws, ws_bytes, s);
+  if (st != GSX_OK) return st;
+  return binning_status(ws, n, capacity, n_tiles_w, n_tiles_h, n_keys_host, nullptr, s);
 }
 
 }  // namespace gsx

@@ -107,6 +107,12 @@ int launch_raster_backward(const RasterArgs &a, int C, cudaStream_t s);
 // Binning.  rect_tl/rect_br point at int32 pairs with `rect_stride` ints per
 // Gaussian (4 for packed [n,4] rects, 2 for separate [n,2] arrays).
 size_t binning_workspace_bytes(int64_t n, int64_t cap, int64_t n_tiles);
+int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
+                      int32_t rect_stride, const int32_t *counts, const float *depth,
+                      int32_t n_tiles_w, int32_t n_tiles_h, int64_t capacity, int32_t *ids,
+                      int32_t *start, int32_t *end, void *ws, size_t ws_bytes, cudaStream_t s);
+int binning_status(const void *ws, int64_t n, int64_t capacity, int32_t n_tiles_w,
+                   int32_t n_tiles_h, int64_t *n_keys_host, uint32_t *flags_host, cudaStream_t s);
 int run_binning(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
                 int32_t rect_stride, const int32_t *counts, const float *depth,
                 int32_t n_tiles_w, int32_t n_tiles_h, int64_t capacity,

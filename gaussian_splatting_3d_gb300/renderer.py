@@ -135,7 +135,7 @@ def project(mean, qvec, log_scale, alpha_logit, gcam, settings: RasterSettings,
 
 
 def bin_gaussians(pr: Projected, n_tiles_w: int, n_tiles_h: int, key_hint: int | None = None):
-    """Sorted Gaussian ids per tile: returns (ids[K], start[T], end[T], K)."""
+    """Sorted Gaussian ids per tile (synchronising): returns (ids[K], start[T], end[T], K)."""
     n = pr.counts.shape[0]
     dev = pr.counts.device
     T = n_tiles_w * n_tiles_h
@@ -156,6 +156,30 @@ def bin_gaussians(pr: Projected, n_tiles_w: int, n_tiles_h: int, key_hint: int |
         K = int(k.value)
         return buf.ids[:K].clone() if K > 0 else buf.ids[:0].clone(), start, end, K
     raise _lib.GsxCapacityError(_lib.GSX_ERR_CAPACITY, "gsx_bin_gaussians", "could not size the key buffer")
+
+
+def bin_gaussians_async(pr: Projected, n_tiles_w: int, n_tiles_h: int, capacity: int):
+    """Enqueue the binning without synchronising: returns (ids[capacity],
+    start, end); binning_status() later gives the key count."""
+    n = pr.counts.shape[0]
+    dev = pr.counts.device
+    T = n_tiles_w * n_tiles_h
+    buf = _bin_buffers(dev).ensure(n, capacity, T)
+    ids = torch.empty((max(capacity, 1),), dtype=torch.int32, device=dev)
+    start = torch.empty((T,), dtype=torch.int32, device=dev)
+    end = torch.empty((T,), dtype=torch.int32, device=dev)
+    _lib.call("gsx_bin_gaussians_async", n, ptr(pr.rect), ptr(pr.counts), ptr(pr.depth), n_tiles_w, n_tiles_h,
+              capacity, ptr(ids), ptr(start), ptr(end), ptr(buf.ws), buf.ws.numel(), stream_handle(dev))
+    return ids, start, end
+
+
+def binning_status(dev, n: int, capacity: int, n_tiles_w: int, n_tiles_h: int):
+    """(status, key count) of the last asynchronous binning on `dev` (synchronises)."""
+    buf = _bin_buffers(dev)
+    k = ctypes.c_int64(0)
+    st = _lib.load().gsx_binning_status(ptr(buf.ws), n, capacity, n_tiles_w, n_tiles_h, ctypes.byref(k),
+                                        stream_handle(dev))
+    return st, int(k.value)
 
 
 def _raster_params(cam: CameraInfo, settings: RasterSettings, C: int, sh_stride: int) -> GsxRasterParams:
@@ -182,6 +206,7 @@ class ViewPipeline:
 
     def __init__(self, device=None):
         self.device = torch.device(device or "cuda")
+        self.key_capacity = 0  # grows to ~1.25x the largest key count seen
 
     def forward(self, mean, qvec, log_scale, sh, alpha_logit, c2w_np, cam: CameraInfo,
                 settings: RasterSettings, timer=None):
@@ -194,19 +219,33 @@ class ViewPipeline:
         with ev("project"):
             pr = project(mean, qvec, log_scale, alpha_logit, gcam, settings)
         ntw, nth = settings.tiles(cam)
-        with ev("binning"):
-            ids, start, end, K = bin_gaussians(pr, ntw, nth)
         topleft = torch.tensor(cam.topleft(), dtype=torch.float32).to(dev, non_blocking=True)
         c2w_dev = torch.from_numpy(np.ascontiguousarray(c2w_np, dtype=np.float32)).reshape(3, 4).to(
             dev, non_blocking=True)
         out = torch.empty((cam.h, cam.w, 3), dtype=torch.float32, device=dev)
         params = _raster_params(cam, settings, C, sh_stride)
-        with ev("raster_fwd"):
-            _lib.call("gsx_render_forward", ctypes.byref(params), n, K, ptr(pr.mean2d), ptr(pr.cov2d), ptr(sh),
-                      ptr(pr.alpha), ptr(start), ptr(end), ptr(ids), ptr(topleft), ptr(c2w_dev), ptr(out),
-                      stream_handle(dev))
-        return dict(pr=pr, ids=ids, start=start, end=end, K=K, topleft=topleft, c2w_dev=c2w_dev, out=out,
-                    params=params, gcam=gcam)
+        cap = max(self.key_capacity, 1 << 16)
+        for _ in range(3):
+            with ev("binning"):
+                ids, start, end = bin_gaussians_async(pr, ntw, nth, cap)
+            with ev("raster_fwd"):
+                _lib.call("gsx_render_forward", ctypes.byref(params), n, cap, ptr(pr.mean2d), ptr(pr.cov2d),
+                          ptr(sh), ptr(pr.alpha), ptr(start), ptr(end), ptr(ids), ptr(topleft), ptr(c2w_dev),
+                          ptr(out), stream_handle(dev))
+            st, K = binning_status(dev, n, cap, ntw, nth)
+            if st == _lib.GSX_ERR_CAPACITY:
+                cap = int(K * 1.25) + 4096
+                self.key_capacity = cap
+                continue
+            _lib.check(st, "gsx_bin_gaussians_async")
+            break
+        else:
+            raise _lib.GsxCapacityError(_lib.GSX_ERR_CAPACITY, "binning", "could not size the key buffer")
+        # keep the capacity near 1.25 K so the sort grids stay small
+        if K * 2 < self.key_capacity:
+            self.key_capacity = max(int(K * 1.25) + 4096, 1 << 16)
+        return dict(pr=pr, ids=ids, start=start, end=end, K=K, cap=cap, topleft=topleft, c2w_dev=c2w_dev,
+                    out=out, params=params, gcam=gcam)
 
     def backward(self, state, mean, qvec, log_scale, sh, alpha_logit, grad_out, timer=None):
         dev = mean.device
@@ -219,7 +258,7 @@ class ViewPipeline:
         g_alpha = torch.zeros((n,), dtype=torch.float32, device=dev)
         g_sh = torch.zeros_like(sh)
         with ev("raster_bwd"):
-            _lib.call("gsx_render_backward", ctypes.byref(state["params"]), n, state["K"], ptr(pr.mean2d),
+            _lib.call("gsx_render_backward", ctypes.byref(state["params"]), n, state["cap"], ptr(pr.mean2d),
                       ptr(pr.cov2d), ptr(sh), ptr(pr.alpha), ptr(state["start"]), ptr(state["end"]),
                       ptr(state["ids"]), ptr(state["topleft"]), ptr(state["c2w_dev"]), ptr(state["out"]),
                       ptr(grad_out), ptr(g_mean2d), ptr(g_cov2d), ptr(g_sh), ptr(g_alpha), stream_handle(dev))

@@ -188,6 +188,22 @@ int gsx_bin_gaussians(int64_t n, const int32_t *rect, const int32_t *counts,
                       int32_t *end, int64_t *n_keys_out, void *workspace,
                       size_t workspace_bytes, void *stream);
 
+/*
+ * The same binning without any host synchronisation (capturable in a CUDA
+ * graph): keys beyond key_capacity are not written, and the key total and
+ * error bits stay in the workspace.  gsx_binning_status reads them later
+ * (synchronising `stream`) and returns GSX_ERR_CAPACITY if the capacity was
+ * too small, in which case the lists are incomplete.
+ */
+int gsx_bin_gaussians_async(int64_t n, const int32_t *rect, const int32_t *counts,
+                            const float *depth, int32_t n_tiles_w, int32_t n_tiles_h,
+                            int64_t key_capacity, int32_t *gaussian_ids, int32_t *start,
+                            int32_t *end, void *workspace, size_t workspace_bytes,
+                            void *stream);
+int gsx_binning_status(const void *workspace, int64_t n_gaussians, int64_t key_capacity,
+                       int32_t n_tiles_w, int32_t n_tiles_h, int64_t *n_keys_out,
+                       void *stream);
+
 /* Raster parameters of the fused path. */
 typedef struct gsx_raster_params {
   int32_t width, height;

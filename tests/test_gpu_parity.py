@@ -275,3 +275,19 @@ def test_sh_order_below_stored_coefficients():
     g = got["grads"]["sh"]
     assert np.all(g[..., 4:] == 0)
     assert rel_err(g[..., :4], ref["param_grads"]["sh"]) <= GRAD_REL
+
+
+def test_pipeline_grows_key_capacity_without_losing_parity():
+    """The fused forward sizes the key lists by a capacity and checks the true
+    count once at the end; a first call with far more keys than the initial
+    capacity (65,536) must re-run and still match the oracle."""
+    wl = S.custom_workload(6000, 320, 240, 1, seed=23, log_scale_mu=-1.8)
+    ref = oracle_view(wl)
+    assert ref["bins"]["K"] > (1 << 16)
+    renderer._pipelines.clear()
+    got = gpu_pipeline(wl)
+    assert_image_close(got["image"], ref["image"])
+    for k, g in got["grads"].items():
+        assert rel_err(g, ref["param_grads"][k]) <= GRAD_REL, k
+    pipe = renderer._pipelines[(dev().type, dev().index)]
+    assert pipe.key_capacity >= ref["bins"]["K"]
