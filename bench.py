@@ -338,13 +338,78 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args):
+    """Batched views/s (fwd+bwd) for the multi-view workload, against plain
+    per-view launches of the same views (identical images)."""
+    import torch
+
+    from gaussian_splatting_3d_gb300 import batch as B, renderer, scene as S
+
+    dev = torch.device("cuda", 0)
+    wl = S.batch_workload(n=args.n_batch, n_views=args.views)
+    sc = B.Scene.from_arrays(wl.scene, dev)
+    specs = [B.ViewSpec(0, v.c2w, v.cam) for v in wl.views]
+    best, tune = B.autotune_tile([sc], specs, reps=1, device=dev)
+    st = renderer.RasterSettings(tile_w=best[0], tile_h=best[1])
+    bp = B.BatchPipeline(dev, st).plan([sc], specs)
+    gen = torch.Generator(device="cpu").manual_seed(0)
+    for g in bp.grad_outs:
+        g.copy_(torch.rand(g.shape, generator=gen))
+    bp.capture()
+    for _ in range(args.warmup):
+        bp.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        bp.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    ms_batch = e0.elapsed_time(e1) / args.steps
+    # plain per-view launches of the same views
+    pipe = renderer.ViewPipeline(dev)
+    params = [sc.mean, sc.qvec, sc.log_scale, sc.sh, sc.alpha_logit]
+
+    def per_view_step():
+        for i, v in enumerate(specs):
+            s = pipe.forward(*params, v.c2w, v.cam, st)
+            pipe.backward(s, *params, bp.grad_outs[i])
+        return s
+
+    for _ in range(max(1, args.warmup // 2)):
+        per_view_step()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(max(1, args.steps // 2)):
+        per_view_step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms_plain = e0.elapsed_time(e1) / max(1, args.steps // 2)
+    same = all(torch.equal(bp.images[i], pipe.forward(*params, v.c2w, v.cam, st)["out"]) for i, v in
+               enumerate(specs[:3]))
+    V = len(specs)
+    line = {
+        "metric": f"batched views/s (fwd+bwd, {V} views, {wl.scene.n} Gaussians)",
+        "value": round(V / (ms_batch * 1e-3), 2), "unit": "views/s", "higher_is_better": True,
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_batch, 3),
+        "plain_per_view_views_per_s": round(V / (ms_plain * 1e-3), 2),
+        "speedup_vs_plain": round(ms_plain / ms_batch, 3), "identical_images_first3": bool(same),
+        "tile": list(best), "autotune_ms": {f"{k[0]}x{k[1]}": round(v, 3) for k, v in tune.items()},
+        "keys": int(bp.n_keys), "dtype": "f32", "data": "synthetic (seeded PCG64)",
+        "config": {"workload": "batch: 32 views cycling 800x800/1280x720/1920x1080, SH degree 3, CUDA graph"},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gsx", choices=["gsx", "reference"])
-    ap.add_argument("--workload", default="headline", choices=["headline", "small"])
+    ap.add_argument("--workload", default="headline", choices=["headline", "small", "batch"])
+    ap.add_argument("--views", type=int, default=32)
+    ap.add_argument("--n-batch", type=int, default=500_000)
     ap.add_argument("--n", type=int, default=1_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-frac", type=float, default=1.0 / 8.0)
@@ -353,6 +418,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_gsx(args)
 

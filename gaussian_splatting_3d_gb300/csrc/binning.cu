@@ -239,7 +239,8 @@ __global__ void __launch_bounds__(kThreads)
     emit_kernel(const uint32_t *__restrict__ order, uint32_t n,
                 const int32_t *__restrict__ rect_tl, const int32_t *__restrict__ rect_br,
                 int rect_stride, const int32_t *__restrict__ counts, int32_t n_tiles_w,
-                int32_t n_tiles_h, uint32_t *__restrict__ tile_out, uint32_t *__restrict__ id_out,
+                int32_t n_tiles_h, const gsx_batch_view *__restrict__ views, int32_t n_views,
+                uint32_t *__restrict__ tile_out, uint32_t *__restrict__ id_out,
                 unsigned long long capacity, unsigned long long *status,
                 uint32_t *chunk_counter, unsigned long long *total_out, uint32_t *k_eff,
                 uint32_t *error) {
@@ -318,14 +319,28 @@ __global__ void __launch_bounds__(kThreads)
     const int32_t *tl = rect_tl + (size_t)g * rect_stride;
     const int32_t *br = rect_br + (size_t)g * rect_stride;
     if (rect_count(tl, br) != cnt[j]) atomicOr(error, kErrCount);
-    const bool in_grid = tl[0] >= 0 && tl[1] >= 0 && br[0] < n_tiles_w && br[1] < n_tiles_h;
+    // tiles of this item's image: one image, or the item's view in a batch
+    int32_t ntw = n_tiles_w, nth = n_tiles_h;
+    uint32_t tile_base = 0;
+    if (views) {
+      int lo = 0, hi = n_views - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (views[mid].item_offset <= (int64_t)g) lo = mid;
+        else hi = mid - 1;
+      }
+      ntw = views[lo].n_tiles_w;
+      nth = views[lo].n_tiles_h;
+      tile_base = (uint32_t)views[lo].tile_offset;
+    }
+    const bool in_grid = tl[0] >= 0 && tl[1] >= 0 && br[0] < ntw && br[1] < nth;
     if (!in_grid) atomicOr(error, kErrRange);
     if (off >= capacity) break;  // the count is known from the scan; nothing more fits
     const unsigned long long stop =
         off + (unsigned long long)cnt[j] < capacity ? off + (unsigned long long)cnt[j] : capacity;
     for (int32_t y = tl[1]; y <= br[1] && off < stop; ++y)
       for (int32_t x = tl[0]; x <= br[0] && off < stop; ++x) {
-        tile_out[off] = in_grid ? (uint32_t)(y * n_tiles_w + x) : 0xffffffffu;
+        tile_out[off] = in_grid ? tile_base + (uint32_t)(y * ntw + x) : 0xffffffffu;
         id_out[off] = g;
         ++off;
       }
@@ -447,8 +462,9 @@ size_t binning_workspace_bytes(int64_t n, int64_t cap, int64_t n_tiles) {
 int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
                       int32_t rect_stride, const int32_t *counts, const float *depth,
                       int32_t n_tiles_w, int32_t n_tiles_h, int64_t capacity, int32_t *ids,
-                      int32_t *start, int32_t *end, void *ws, size_t ws_bytes, cudaStream_t s) {
-  const int64_t n_tiles = (int64_t)n_tiles_w * n_tiles_h;
+                      int32_t *start, int32_t *end, void *ws, size_t ws_bytes, cudaStream_t s,
+                      const gsx_batch_view *views, int32_t n_views, int64_t total_tiles) {
+  const int64_t n_tiles = views ? total_tiles : (int64_t)n_tiles_w * n_tiles_h;
   Workspace w = carve_ws(ws, n, capacity);
   if (ws_bytes < w.bytes) {
     set_error("binning workspace too small: %zu < %zu bytes", ws_bytes, w.bytes);
@@ -475,7 +491,8 @@ int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
   if (e != cudaSuccess) return cuda_status(e, "memset emission state");
   count_launches(1);
   emit_kernel<<<emit_chunks, kThreads, 0, s>>>(
-      w.dvals[1], nn, rect_tl, rect_br, rect_stride, counts, n_tiles_w, n_tiles_h, w.tkeys[0],
+      w.dvals[1], nn, rect_tl, rect_br, rect_stride, counts, n_tiles_w, n_tiles_h, views, n_views,
+      w.tkeys[0],
       w.tvals[0], (unsigned long long)capacity, w.emit_status, w.counters + 8, w.total, w.k_eff,
       w.error);
   e = cudaGetLastError();

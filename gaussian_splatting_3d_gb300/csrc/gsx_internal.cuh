@@ -86,6 +86,14 @@ int launch_project_backward(int64_t n, const float *mean, const float *qvec,
                             const float *g_alpha, float *g_mean, float *g_qvec,
                             float *g_logs, float *g_alpha_logit, cudaStream_t s);
 
+int launch_project_forward_batch(const gsx_batch_view *views, int32_t n_views, int64_t max_n,
+                                 float frustum_radius, float tile_radius, float *mean2d,
+                                 float *cov2d, float *depth, float *alpha, int32_t *rect,
+                                 int32_t *counts, cudaStream_t s);
+int launch_project_backward_batch(const gsx_batch_view *views, int32_t n_views, int64_t n,
+                                  const int32_t *counts, const float *g_mean2d,
+                                  const float *g_cov2d, const float *g_alpha, cudaStream_t s);
+
 struct RasterArgs {
   int64_t n, n_keys;  // Gaussians and list entries: bounds for start/end/ids
   int32_t width, height, tile_w, tile_h, n_tiles_w, n_tiles_h;
@@ -100,9 +108,16 @@ struct RasterArgs {
   // backward only
   const float *final_img, *grad_out;
   float *g_mean2d, *g_cov2d, *g_sh, *g_alpha;
+  // batched passes: per-view table in device memory (nullptr for one view)
+  const gsx_batch_view *views;
+  int32_t n_views;
 };
 int launch_raster_forward(const RasterArgs &a, int C, cudaStream_t s);
 int launch_raster_backward(const RasterArgs &a, int C, cudaStream_t s);
+// Batched: a.views/a.n_views set, grid = total tiles (all views share the tile
+// shape and SH order; the per-view fields of `a` are ignored).
+int launch_raster_forward_batch(const RasterArgs &a, int C, int64_t total_tiles, cudaStream_t s);
+int launch_raster_backward_batch(const RasterArgs &a, int C, int64_t total_tiles, cudaStream_t s);
 
 // Binning.  rect_tl/rect_br point at int32 pairs with `rect_stride` ints per
 // Gaussian (4 for packed [n,4] rects, 2 for separate [n,2] arrays).
@@ -110,7 +125,9 @@ size_t binning_workspace_bytes(int64_t n, int64_t cap, int64_t n_tiles);
 int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
                       int32_t rect_stride, const int32_t *counts, const float *depth,
                       int32_t n_tiles_w, int32_t n_tiles_h, int64_t capacity, int32_t *ids,
-                      int32_t *start, int32_t *end, void *ws, size_t ws_bytes, cudaStream_t s);
+                      int32_t *start, int32_t *end, void *ws, size_t ws_bytes, cudaStream_t s,
+                      const gsx_batch_view *views = nullptr, int32_t n_views = 0,
+                      int64_t total_tiles = 0);
 int binning_status(const void *ws, int64_t n, int64_t capacity, int32_t n_tiles_w,
                    int32_t n_tiles_h, int64_t *n_keys_host, uint32_t *flags_host, cudaStream_t s);
 int run_binning(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,

@@ -88,18 +88,14 @@ __device__ __forceinline__ void quat_rot(const float4 q, Rot &o) {
   o.R[2][2] = 1.0f - (txx + tyy);
 }
 
-__global__ void __launch_bounds__(256)
-    project_forward_kernel(int64_t n, const float *__restrict__ mean,
-                           const float4 *__restrict__ qvec,
-                           const float *__restrict__ log_scale,
-                           const float *__restrict__ alpha_logit, const ProjCam cam,
-                           float frustum_radius, float tile_radius, int32_t tile_w,
-                           int32_t tile_h, int32_t activated,
-                           float2 *__restrict__ mean2d, float4 *__restrict__ cov2d,
-                           float *__restrict__ depth, float *__restrict__ alpha,
-                           int4 *__restrict__ rect, int32_t *__restrict__ counts) {
-  int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= n) return;
+// One Gaussian through activation, cull, projection, covariance and AABB.
+__device__ __forceinline__ void project_one(const ProjCam &cam, const float *__restrict__ mean,
+                                            float4 q, const float *__restrict__ log_scale,
+                                            const float *__restrict__ alpha_logit, int64_t g,
+                                            float frustum_radius, float tile_radius, int32_t tile_w,
+                                            int32_t tile_h, int32_t activated, float2 &o_mean2d,
+                                            float4 &o_cov2d, float &o_depth, float &o_alpha,
+                                            int4 &o_rect, int32_t &o_count) {
   const float m0 = mean[3 * g], m1 = mean[3 * g + 1], m2 = mean[3 * g + 2];
   float s0 = log_scale[3 * g], s1 = log_scale[3 * g + 1], s2 = log_scale[3 * g + 2];
   if (!activated) {
@@ -107,14 +103,14 @@ __global__ void __launch_bounds__(256)
     s1 = gsx_expf(s1);
     s2 = gsx_expf(s2);
   }
-  alpha[g] = alpha_logit ? gsx_sigmoidf(alpha_logit[g]) : 0.0f;
+  o_alpha = alpha_logit ? gsx_sigmoidf(alpha_logit[g]) : 0.0f;
   float r = fmaxf(fmaxf(s0, s1), s2) * frustum_radius;
   if (!sphere_in_frustum(m0, m1, m2, r, cam.normals, cam.pts)) {
-    counts[g] = 0;
-    rect[g] = make_int4(0, 0, -1, -1);
-    mean2d[g] = make_float2(0.0f, 0.0f);
-    cov2d[g] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    depth[g] = 0.0f;
+    o_count = 0;
+    o_rect = make_int4(0, 0, -1, -1);
+    o_mean2d = make_float2(0.0f, 0.0f);
+    o_cov2d = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    o_depth = 0.0f;
     return;
   }
   // p = W (x - t)
@@ -124,7 +120,7 @@ __global__ void __launch_bounds__(256)
   for (int i = 0; i < 3; ++i)
     p[i] = fmaf(cam.W[i][2], v2, fmaf(cam.W[i][1], v1, cam.W[i][0] * v0));
   Rot rot;
-  quat_rot(qvec[g], rot);
+  quat_rot(q, rot);
   const float sv[3] = {s0, s1, s2};
   float M[3][3];
 #pragma unroll
@@ -159,9 +155,9 @@ __global__ void __launch_bounds__(256)
     for (int l = 0; l < 2; ++l)
       cv[i][l] = fmaf(T[i][2], A[l][2], fmaf(T[i][1], A[l][1], T[i][0] * A[l][0]));
   float mx = p[0] / p[2], my = p[1] / p[2];
-  mean2d[g] = make_float2(mx, my);
-  cov2d[g] = make_float4(cv[0][0], cv[0][1], cv[1][0], cv[1][1]);
-  depth[g] = p[2];
+  o_mean2d = make_float2(mx, my);
+  o_cov2d = make_float4(cv[0][0], cv[0][1], cv[1][0], cv[1][1]);
+  o_depth = p[2];
   float ax = sqrtf(tile_radius * cv[0][0]);
   float ay = sqrtf(tile_radius * cv[1][1]);
   float tlx = mx - ax, tly = my - ay, brx = mx + ax, bry = my + ay;
@@ -171,46 +167,82 @@ __global__ void __launch_bounds__(256)
   int32_t itly = min(max(f2i_sat(ptly), 0), cam.height - 1) / tile_h;
   int32_t ibrx = min(max(f2i_sat(pbrx), 0), cam.width - 1) / tile_w;
   int32_t ibry = min(max(f2i_sat(pbry), 0), cam.height - 1) / tile_h;
-  rect[g] = make_int4(itlx, itly, ibrx, ibry);
-  counts[g] = (ibrx - itlx + 1) * (ibry - itly + 1);
+  o_rect = make_int4(itlx, itly, ibrx, ibry);
+  o_count = (ibrx - itlx + 1) * (ibry - itly + 1);
 }
 
-// Parity-mode backward of the projection (depth detached, J constant).
 __global__ void __launch_bounds__(256)
-    project_backward_kernel(int64_t n, const float *__restrict__ mean,
-                            const float4 *__restrict__ qvec,
-                            const float *__restrict__ log_scale,
-                            const float *__restrict__ alpha_logit, const ProjCam cam,
-                            const int32_t *__restrict__ counts,
-                            const float2 *__restrict__ g_mean2d,
-                            const float4 *__restrict__ g_cov2d,
-                            const float *__restrict__ g_alpha,
-                            float *__restrict__ g_mean, float4 *__restrict__ g_qvec,
-                            float *__restrict__ g_logs,
-                            float *__restrict__ g_alpha_logit) {
+    project_forward_kernel(int64_t n, const float *__restrict__ mean,
+                           const float4 *__restrict__ qvec,
+                           const float *__restrict__ log_scale,
+                           const float *__restrict__ alpha_logit, const ProjCam cam,
+                           float frustum_radius, float tile_radius, int32_t tile_w,
+                           int32_t tile_h, int32_t activated,
+                           float2 *__restrict__ mean2d, float4 *__restrict__ cov2d,
+                           float *__restrict__ depth, float *__restrict__ alpha,
+                           int4 *__restrict__ rect, int32_t *__restrict__ counts) {
   int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n) return;
-  if (counts[g] == 0) {
-    g_mean[3 * g] = 0.0f;
-    g_mean[3 * g + 1] = 0.0f;
-    g_mean[3 * g + 2] = 0.0f;
-    g_logs[3 * g] = 0.0f;
-    g_logs[3 * g + 1] = 0.0f;
-    g_logs[3 * g + 2] = 0.0f;
-    g_qvec[g] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    g_alpha_logit[g] = 0.0f;
-    return;
+  project_one(cam, mean, qvec[g], log_scale, alpha_logit, g, frustum_radius, tile_radius, tile_w,
+              tile_h, activated, mean2d[g], cov2d[g], depth[g], alpha[g], rect[g], counts[g]);
+}
+
+__device__ __forceinline__ ProjCam proj_cam_of(const gsx_camera &c) {
+  ProjCam p;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) p.W[i][j] = c.c2w[4 * j + i];
+  p.t[0] = c.c2w[3];
+  p.t[1] = c.c2w[7];
+  p.t[2] = c.c2w[11];
+  p.fx = c.fx;
+  p.fy = c.fy;
+  p.cx = c.cx;
+  p.cy = c.cy;
+  p.width = c.width;
+  p.height = c.height;
+#pragma unroll
+  for (int k = 0; k < 18; ++k) {
+    p.normals[k] = c.frustum_normals[k];
+    p.pts[k] = c.frustum_pts[k];
   }
-  const float m0 = mean[3 * g], m1 = mean[3 * g + 1], m2 = mean[3 * g + 2];
+  return p;
+}
+
+// All views of a batch: grid (Gaussian blocks, view); item = view's item
+// offset + Gaussian index.
+__global__ void __launch_bounds__(256)
+    project_forward_batch_kernel(const gsx_batch_view *__restrict__ views, float frustum_radius,
+                                 float tile_radius, float2 *__restrict__ mean2d,
+                                 float4 *__restrict__ cov2d, float *__restrict__ depth,
+                                 float *__restrict__ alpha, int4 *__restrict__ rect,
+                                 int32_t *__restrict__ counts) {
+  const gsx_batch_view &v = views[blockIdx.y];
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= v.n_gaussians) return;
+  const int64_t item = v.item_offset + g;
+  const ProjCam cam = proj_cam_of(v.cam);
+  const float4 q = reinterpret_cast<const float4 *>(v.qvec)[g];
+  project_one(cam, v.mean, q, v.log_scale, v.alpha_logit, g, frustum_radius, tile_radius, v.tile_w,
+              v.tile_h, 0, mean2d[item], cov2d[item], depth[item], alpha[item], rect[item],
+              counts[item]);
+}
+
+// Parity-mode backward of the projection (depth detached, J constant):
+// the part that depends on the view.  Adds dL/dmean (through
+// mean2d = p_xy / p_z) into gm and dL/dSigma = A^T Gc A into GS.
+__device__ __forceinline__ void accum_view_grad(const ProjCam &cam, float m0, float m1, float m2,
+                                                float2 gm2, float4 gc, float (&gm)[3],
+                                                float (&GS)[3][3]) {
   float v0 = m0 - cam.t[0], v1 = m1 - cam.t[1], v2 = m2 - cam.t[2];
   float p[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i)
     p[i] = fmaf(cam.W[i][2], v2, fmaf(cam.W[i][1], v1, cam.W[i][0] * v0));
-  const float2 gm = g_mean2d[g];
-  const float gp0 = gm.x / p[2], gp1 = gm.y / p[2];
+  const float gp0 = gm2.x / p[2], gp1 = gm2.y / p[2];
 #pragma unroll
-  for (int j = 0; j < 3; ++j) g_mean[3 * g + j] = fmaf(cam.W[1][j], gp1, cam.W[0][j] * gp0);
+  for (int j = 0; j < 3; ++j) gm[j] += fmaf(cam.W[1][j], gp1, cam.W[0][j] * gp0);
   float iz = 1.0f / p[2];
   float j02 = (-p[0] / p[2]) / p[2];
   float j12 = (-p[1] / p[2]) / p[2];
@@ -220,21 +252,27 @@ __global__ void __launch_bounds__(256)
     A[0][k] = fmaf(j02, cam.W[2][k], iz * cam.W[0][k]);
     A[1][k] = fmaf(j12, cam.W[2][k], iz * cam.W[1][k]);
   }
-  const float4 gc = g_cov2d[g];
-  // B = Gc A (2x3); GS = A^T B (3x3)
   float B[2][3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     B[0][k] = fmaf(gc.y, A[1][k], gc.x * A[0][k]);
     B[1][k] = fmaf(gc.w, A[1][k], gc.z * A[0][k]);
   }
-  float GS[3][3];
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
-    for (int k = 0; k < 3; ++k) GS[i][k] = fmaf(A[1][i], B[1][k], A[0][i] * B[0][k]);
+    for (int k = 0; k < 3; ++k) GS[i][k] += fmaf(A[1][i], B[1][k], A[0][i] * B[0][k]);
+}
+
+// The view-independent part: dL/dSigma -> quaternion and log-scale, and the
+// opacity logit.
+__device__ __forceinline__ void finish_param_grad(float4 q, const float *__restrict__ log_scale,
+                                                  float alpha_logit, int64_t g,
+                                                  const float (&GS)[3][3], float g_alpha,
+                                                  float *__restrict__ g_logs, float4 &g_q,
+                                                  float &g_al) {
   Rot rot;
-  quat_rot(qvec[g], rot);
+  quat_rot(q, rot);
   float s[3];
   s[0] = gsx_expf(log_scale[3 * g]);
   s[1] = gsx_expf(log_scale[3 * g + 1]);
@@ -267,19 +305,96 @@ __global__ void __launch_bounds__(256)
                      z * GR[1][2] - w * GR[2][0] + z * GR[2][1] - 2.0f * y * GR[2][2]);
   float gz = 2.0f * (-2.0f * z * GR[0][0] - w * GR[0][1] + x * GR[0][2] + w * GR[1][0] -
                      2.0f * z * GR[1][1] + y * GR[1][2] + x * GR[2][0] + y * GR[2][1]);
-  const float4 q = qvec[g];
   float nq = sqrtf(fmaf(q.w, q.w, fmaf(q.z, q.z, fmaf(q.y, q.y, q.x * q.x))));
-  float4 gq;
   if (nq > 1e-12f) {
     float dp = gw * w + gx * x + gy * y + gz * z;
-    gq = make_float4((gw - dp * w) / nq, (gx - dp * x) / nq, (gy - dp * y) / nq,
-                     (gz - dp * z) / nq);
+    g_q = make_float4((gw - dp * w) / nq, (gx - dp * x) / nq, (gy - dp * y) / nq,
+                      (gz - dp * z) / nq);
   } else {
-    gq = make_float4(gw / 1e-12f, gx / 1e-12f, gy / 1e-12f, gz / 1e-12f);
+    g_q = make_float4(gw / 1e-12f, gx / 1e-12f, gy / 1e-12f, gz / 1e-12f);
   }
+  float a = gsx_sigmoidf(alpha_logit);
+  g_al = g_alpha * (a * (1.0f - a));
+}
+
+__global__ void __launch_bounds__(256)
+    project_backward_kernel(int64_t n, const float *__restrict__ mean,
+                            const float4 *__restrict__ qvec,
+                            const float *__restrict__ log_scale,
+                            const float *__restrict__ alpha_logit, const ProjCam cam,
+                            const int32_t *__restrict__ counts,
+                            const float2 *__restrict__ g_mean2d,
+                            const float4 *__restrict__ g_cov2d,
+                            const float *__restrict__ g_alpha,
+                            float *__restrict__ g_mean, float4 *__restrict__ g_qvec,
+                            float *__restrict__ g_logs,
+                            float *__restrict__ g_alpha_logit) {
+  int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n) return;
+  if (counts[g] == 0) {
+    g_mean[3 * g] = 0.0f;
+    g_mean[3 * g + 1] = 0.0f;
+    g_mean[3 * g + 2] = 0.0f;
+    g_logs[3 * g] = 0.0f;
+    g_logs[3 * g + 1] = 0.0f;
+    g_logs[3 * g + 2] = 0.0f;
+    g_qvec[g] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    g_alpha_logit[g] = 0.0f;
+    return;
+  }
+  float gm[3] = {0.0f, 0.0f, 0.0f};
+  float GS[3][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};
+  accum_view_grad(cam, mean[3 * g], mean[3 * g + 1], mean[3 * g + 2], g_mean2d[g], g_cov2d[g], gm,
+                  GS);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) g_mean[3 * g + j] = gm[j];
+  finish_param_grad(qvec[g], log_scale, alpha_logit[g], g, GS, g_alpha[g], g_logs, g_qvec[g],
+                    g_alpha_logit[g]);
+}
+
+// Batched backward for views that share one scene (views[0]'s): per
+// Gaussian, sum the view-dependent parts over every view that saw it, then
+// back-propagate once through the rotation, scales and opacity.
+__global__ void __launch_bounds__(256)
+    project_backward_batch_kernel(const gsx_batch_view *__restrict__ views, int32_t n_views,
+                                  const int32_t *__restrict__ counts,
+                                  const float2 *__restrict__ g_mean2d,
+                                  const float4 *__restrict__ g_cov2d,
+                                  const float *__restrict__ g_alpha) {
+  const gsx_batch_view &v0 = views[0];
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= v0.n_gaussians) return;
+  const float m0 = v0.mean[3 * g], m1 = v0.mean[3 * g + 1], m2 = v0.mean[3 * g + 2];
+  float gm[3] = {0.0f, 0.0f, 0.0f};
+  float GS[3][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};
+  float ga = 0.0f;
+  bool seen = false;
+  for (int vi = 0; vi < n_views; ++vi) {
+    const int64_t item = views[vi].item_offset + g;
+    if (counts[item] == 0) continue;
+    seen = true;
+    accum_view_grad(proj_cam_of(views[vi].cam), m0, m1, m2, g_mean2d[item], g_cov2d[item], gm, GS);
+    ga += g_alpha[item];
+  }
+  float4 *g_qvec = reinterpret_cast<float4 *>(v0.g_qvec);
+  if (!seen) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      v0.g_mean[3 * g + j] = 0.0f;
+      v0.g_log_scale[3 * g + j] = 0.0f;
+    }
+    g_qvec[g] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    v0.g_alpha_logit[g] = 0.0f;
+    return;
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) v0.g_mean[3 * g + j] = gm[j];
+  float4 gq;
+  float gal;
+  finish_param_grad(reinterpret_cast<const float4 *>(v0.qvec)[g], v0.log_scale,
+                    v0.alpha_logit[g], g, GS, ga, v0.g_log_scale, gq, gal);
   g_qvec[g] = gq;
-  float a = gsx_sigmoidf(alpha_logit[g]);
-  g_alpha_logit[g] = g_alpha[g] * (a * (1.0f - a));
+  v0.g_alpha_logit[g] = gal;
 }
 
 inline unsigned grid_for(int64_t n, int threads) {
@@ -287,6 +402,29 @@ inline unsigned grid_for(int64_t n, int threads) {
 }
 
 }  // namespace
+
+int launch_project_forward_batch(const gsx_batch_view *views, int32_t n_views, int64_t max_n,
+                                 float frustum_radius, float tile_radius, float *mean2d,
+                                 float *cov2d, float *depth, float *alpha, int32_t *rect,
+                                 int32_t *counts, cudaStream_t s) {
+  if (max_n == 0 || n_views == 0) return GSX_OK;
+  count_launches(1);
+  project_forward_batch_kernel<<<dim3(grid_for(max_n, 256), (unsigned)n_views), 256, 0, s>>>(
+      views, frustum_radius, tile_radius, reinterpret_cast<float2 *>(mean2d),
+      reinterpret_cast<float4 *>(cov2d), depth, alpha, reinterpret_cast<int4 *>(rect), counts);
+  return cuda_status(cudaGetLastError(), "project_forward_batch_kernel launch");
+}
+
+int launch_project_backward_batch(const gsx_batch_view *views, int32_t n_views, int64_t n,
+                                  const int32_t *counts, const float *g_mean2d,
+                                  const float *g_cov2d, const float *g_alpha, cudaStream_t s) {
+  if (n == 0 || n_views == 0) return GSX_OK;
+  count_launches(1);
+  project_backward_batch_kernel<<<grid_for(n, 256), 256, 0, s>>>(
+      views, n_views, counts, reinterpret_cast<const float2 *>(g_mean2d),
+      reinterpret_cast<const float4 *>(g_cov2d), g_alpha);
+  return cuda_status(cudaGetLastError(), "project_backward_batch_kernel launch");
+}
 
 int launch_cull_bsphere(int64_t n, const float *mean, const float *svec,
                         const float *normal, const float *pts, uint8_t *mask,

@@ -130,41 +130,116 @@ __device__ __forceinline__ bool surely_skipped(float radial, float a) {
   return radial > 12.0f && a != -__int_as_float(0x7f800000);
 }
 
+// Per-CTA view of the work: which tile of which image, and where the view's
+// scene and image live.  One view: everything comes from the kernel
+// arguments.  Batched: the global tile number selects the view from the
+// device table (binary search over the tile offsets).
+struct ViewCtx {
+  int gtile;  // tile index in start/end (global over the batch)
+  int tile;   // tile index within the view's image
+  int n_tiles_w, tile_w, tile_h, width, height;
+  float psx, psy;
+  const float *topleft, *c2w;
+  const float *sh;
+  int sh_stride;
+  int64_t item_lo, item_hi;  // items of this view: [item_lo, item_hi)
+  float *out;
+  const float *final_img, *grad_out;
+  float *g_sh;
+  int write_empty;
+};
+
+template <bool BATCHED>
+__device__ __forceinline__ ViewCtx make_ctx(const RasterArgs &a) {
+  ViewCtx c;
+  c.gtile = blockIdx.x;
+  if constexpr (!BATCHED) {
+    c.tile = blockIdx.x;
+    c.n_tiles_w = a.n_tiles_w;
+    c.tile_w = a.tile_w;
+    c.tile_h = a.tile_h;
+    c.width = a.width;
+    c.height = a.height;
+    c.psx = a.psx;
+    c.psy = a.psy;
+    c.topleft = a.topleft;
+    c.c2w = a.c2w;
+    c.sh = a.sh;
+    c.sh_stride = a.sh_stride;
+    c.item_lo = 0;
+    c.item_hi = a.n;
+    c.out = a.out;
+    c.final_img = a.final_img;
+    c.grad_out = a.grad_out;
+    c.g_sh = a.g_sh;
+    c.write_empty = a.write_empty;
+  } else {
+    const int64_t gt = blockIdx.x;
+    int lo = 0, hi = a.n_views - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (a.views[mid].tile_offset <= gt) lo = mid;
+      else hi = mid - 1;
+    }
+    const gsx_batch_view &v = a.views[lo];
+    c.tile = (int)(gt - v.tile_offset);
+    c.n_tiles_w = v.n_tiles_w;
+    c.tile_w = v.tile_w;
+    c.tile_h = v.tile_h;
+    c.width = v.cam.width;
+    c.height = v.cam.height;
+    c.psx = v.pixel_size_x;
+    c.psy = v.pixel_size_y;
+    c.topleft = v.topleft;
+    c.c2w = v.cam.c2w;
+    c.sh = v.sh;
+    c.sh_stride = v.sh_stride;
+    c.item_lo = v.item_offset;
+    c.item_hi = v.item_offset + v.n_gaussians;
+    c.out = v.out;
+    c.final_img = v.out;
+    c.grad_out = v.grad_out;
+    c.g_sh = v.g_sh;
+    c.write_empty = v.write_empty_tiles;
+  }
+  return c;
+}
+
 // Length of a tile's list; 0 for empty tiles (start == -1, as the reference
 // marks them) and for ranges that do not fit in [0, n_keys).
-__device__ __forceinline__ int tile_list_length(const RasterArgs &a, int tile, int s0) {
+__device__ __forceinline__ int tile_list_length(const RasterArgs &a, int gtile, int s0) {
   if (s0 < 0) return 0;
-  const int e = a.end[tile];
+  const int e = a.end[gtile];
   if (e < s0 || (int64_t)e > a.n_keys) return 0;
   return e - s0;
 }
 
 // Pixel of thread t: warps cover 8x4 blocks when the tile allows it (a
 // compact footprint means fewer warps per small Gaussian), else rows.
-__device__ __forceinline__ void pixel_of(const RasterArgs &a, int tile, int t, int &gx, int &gy) {
+__device__ __forceinline__ void pixel_of(const ViewCtx &c, int t, int &gx, int &gy) {
   int lx, ly;
-  if ((a.tile_w & 7) == 0 && (a.tile_h & 3) == 0) {
-    const int w = t >> 5, l = t & 31, bpr = a.tile_w >> 3;
+  if ((c.tile_w & 7) == 0 && (c.tile_h & 3) == 0) {
+    const int w = t >> 5, l = t & 31, bpr = c.tile_w >> 3;
     lx = (w % bpr) * 8 + (l & 7);
     ly = (w / bpr) * 4 + (l >> 3);
   } else {
-    lx = t % a.tile_w;
-    ly = t / a.tile_w;
+    lx = t % c.tile_w;
+    ly = t / c.tile_w;
   }
-  gx = (tile % a.n_tiles_w) * a.tile_w + lx;
-  gy = (tile / a.n_tiles_w) * a.tile_h + ly;
+  gx = (c.tile % c.n_tiles_w) * c.tile_w + lx;
+  gy = (c.tile / c.n_tiles_w) * c.tile_h + ly;
 }
 
 // Normalised coordinates of the first and last pixel centres of a tile that
 // lie inside the image (computed like the pixel positions themselves).
-__device__ __forceinline__ void tile_bounds(const RasterArgs &a, int tile, float &x0, float &x1,
-                                            float &y0, float &y1) {
-  const int gx0 = (tile % a.n_tiles_w) * a.tile_w, gy0 = (tile / a.n_tiles_w) * a.tile_h;
-  const int gx1 = min(gx0 + a.tile_w, a.width) - 1, gy1 = min(gy0 + a.tile_h, a.height) - 1;
-  x0 = fmaf((float)gx0, a.psx, a.topleft[0]);
-  x1 = fmaf((float)gx1, a.psx, a.topleft[0]);
-  y0 = fmaf((float)gy0, a.psy, a.topleft[1]);
-  y1 = fmaf((float)gy1, a.psy, a.topleft[1]);
+__device__ __forceinline__ void tile_bounds(const ViewCtx &c, float &x0, float &x1, float &y0,
+                                            float &y1) {
+  const int gx0 = (c.tile % c.n_tiles_w) * c.tile_w, gy0 = (c.tile / c.n_tiles_w) * c.tile_h;
+  const int gx1 = min(gx0 + c.tile_w, c.width) - 1, gy1 = min(gy0 + c.tile_h, c.height) - 1;
+  x0 = fmaf((float)gx0, c.psx, c.topleft[0]);
+  x1 = fmaf((float)gx1, c.psx, c.topleft[0]);
+  y0 = fmaf((float)gy0, c.psy, c.topleft[1]);
+  y1 = fmaf((float)gy1, c.psy, c.topleft[1]);
   if (x0 > x1) { const float tmp = x0; x0 = x1; x1 = tmp; }
   if (y0 > y1) { const float tmp = y0; y0 = y1; y1 = tmp; }
 }
@@ -229,9 +304,10 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 // Gaussians whose skip box meets the tile's pixel centres (in list order).
 // Requires nb <= blockDim.x.  Returns the number kept.
 template <int C>
-__device__ __forceinline__ int load_batch(const RasterArgs &a, const SmemLayout &L, int first,
-                                          int nb, int t, int nthr, float tx0, float tx1,
-                                          float ty0, float ty1, int *s_wcount) {
+__device__ __forceinline__ int load_batch(const RasterArgs &a, const ViewCtx &ctx,
+                                          const SmemLayout &L, int first, int nb, int t, int nthr,
+                                          float tx0, float tx1, float ty0, float ty1,
+                                          int *s_wcount) {
   constexpr int CC = Sh<C>::CC, CCP = Sh<C>::CCP, GSH = Sh<C>::GSH;
   const int lane = t & 31, warp = t >> 5, nwarps = nthr >> 5;
   bool keep = false;
@@ -241,7 +317,7 @@ __device__ __forceinline__ int load_batch(const RasterArgs &a, const SmemLayout 
   float al = 0.0f;
   if (t < nb) {
     id = a.ids[first + t];
-    if (id >= 0 && id < a.n) {
+    if (id >= ctx.item_lo && id < ctx.item_hi) {
       const float *m = a.mean2d + 2 * (int64_t)id;
       const float *c = a.cov2d + 4 * (int64_t)id;
       mm = make_float2(m[0], m[1]);
@@ -252,7 +328,7 @@ __device__ __forceinline__ int load_batch(const RasterArgs &a, const SmemLayout 
       keep = !drop && !(mm.x + box.x < tx0) && !(mm.x - box.x > tx1) && !(mm.y + box.y < ty0) &&
              !(mm.y - box.y > ty1);
     }
-    // ids outside [0, n) are dropped: no reads of the caller's arrays
+    // ids outside the view's items are dropped: no reads of the caller's arrays
   }
   const unsigned ballot = __ballot_sync(kFull, keep);
   if (lane == 0) s_wcount[warp] = __popc(ballot);
@@ -278,7 +354,8 @@ __device__ __forceinline__ int load_batch(const RasterArgs &a, const SmemLayout 
     int rem = f - j * (3 * CC);
     int ch = rem / CC;
     int k = rem - ch * CC;
-    L.sh[j * GSH + ch * CCP + k] = a.sh[((int64_t)L.ids[j] * 3 + ch) * a.sh_stride + k];
+    const int64_t g = (int64_t)L.ids[j] - ctx.item_lo;  // Gaussian within the view's scene
+    L.sh[j * GSH + ch * CCP + k] = ctx.sh[(g * 3 + ch) * ctx.sh_stride + k];
   }
   __syncthreads();
   return total;
@@ -292,7 +369,7 @@ __device__ __forceinline__ void pack_basis(const float *Y, float2 *Y2) {
     Y2[j] = make_float2(Y[2 * j], 2 * j + 1 < CC ? Y[(2 * j + 1) < CC ? 2 * j + 1 : 0] : 0.0f);
 }
 
-template <int C, int MAXT>
+template <int C, int MAXT, bool BATCHED>
 __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a) {
   constexpr int GSH = Sh<C>::GSH, CCP = Sh<C>::CCP;
   extern __shared__ float4 smem4[];
@@ -301,40 +378,41 @@ __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a
   const int B = a.batch;
   SmemLayout L = carve<C>(reinterpret_cast<float *>(smem4), B);
 
-  const int tile = blockIdx.x;
+  const ViewCtx ctx = make_ctx<BATCHED>(a);
   const int t = threadIdx.x;
   int gx, gy;
-  pixel_of(a, tile, t, gx, gy);
-  const bool inside = t < a.tile_w * a.tile_h && gx < a.width && gy < a.height;
-  const int s0 = a.start[tile];
-  const int n = tile_list_length(a, tile, s0);
+  pixel_of(ctx, t, gx, gy);
+  const bool inside = t < ctx.tile_w * ctx.tile_h && gx < ctx.width && gy < ctx.height;
+  const int s0 = a.start[ctx.gtile];
+  const int n = tile_list_length(a, ctx.gtile, s0);
   if (n <= 0) {
-    if (a.write_empty && inside) {
-      float *dst = a.out + 3 * ((int64_t)gy * a.width + gx);
+    if (ctx.write_empty && inside) {
+      float *dst = ctx.out + 3 * ((int64_t)gy * ctx.width + gx);
       dst[0] = 0.0f;
       dst[1] = 0.0f;
       dst[2] = 0.0f;
     }
     return;
   }
-  const float px = fmaf((float)gx, a.psx, a.topleft[0]);
-  const float py = fmaf((float)gy, a.psy, a.topleft[1]);
+  const float px = fmaf((float)gx, ctx.psx, ctx.topleft[0]);
+  const float py = fmaf((float)gy, ctx.psy, ctx.topleft[1]);
   float2 Y2[Sh<C>::NY2];
   {
     float Y[Sh<C>::CC];
-    sh_basis<C>(a.c2w, px, py, Y);
+    sh_basis<C>(ctx.c2w, px, py, Y);
     pack_basis<C>(Y, Y2);
   }
   float o0 = 0.0f, o1 = 0.0f, o2 = 0.0f, T = 1.0f;
   const float thr = a.T_thresh;
   bool done = !inside;
   float tx0, tx1, ty0, ty1;
-  tile_bounds(a, tile, tx0, tx1, ty0, ty1);
+  tile_bounds(ctx, tx0, tx1, ty0, ty1);
 
   for (int base = 0; base < n; base += B) {
     if (__syncthreads_and(done)) break;
     const int nb = min(B, n - base);
-    const int nk = load_batch<C>(a, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1, s_wcount);
+    const int nk =
+        load_batch<C>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1, s_wcount);
     if (!done) {
       for (int i = 0; i < nk; ++i) {
         if (T < thr) {
@@ -369,7 +447,7 @@ __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a
     }
   }
   if (inside) {
-    float *dst = a.out + 3 * ((int64_t)gy * a.width + gx);
+    float *dst = ctx.out + 3 * ((int64_t)gy * ctx.width + gx);
     dst[0] = o0;
     dst[1] = o1;
     dst[2] = o2;
@@ -461,7 +539,7 @@ __device__ __forceinline__ void flush_sh_group(const float *Ws, const float *Ys,
     }
 }
 
-template <int C, int MAXT>
+template <int C, int MAXT, bool BATCHED>
 __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1)
     raster_backward_kernel(const RasterArgs a) {
   constexpr int CC = Sh<C>::CC, CCP = Sh<C>::CCP, GSH = Sh<C>::GSH;
@@ -478,34 +556,34 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
   int *s_slots = reinterpret_cast<int *>(s_y + nwarps * 32 * kYStride);  // [nwarps][8]
   int *s_touched = s_slots + nwarps * 8;                                  // [B]
 
-  const int tile = blockIdx.x;
+  const ViewCtx ctx = make_ctx<BATCHED>(a);
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   int gx, gy;
-  pixel_of(a, tile, t, gx, gy);
-  const bool inside = t < a.tile_w * a.tile_h && gx < a.width && gy < a.height;
-  const int s0 = a.start[tile];
-  const int n = tile_list_length(a, tile, s0);
+  pixel_of(ctx, t, gx, gy);
+  const bool inside = t < ctx.tile_w * ctx.tile_h && gx < ctx.width && gy < ctx.height;
+  const int s0 = a.start[ctx.gtile];
+  const int n = tile_list_length(a, ctx.gtile, s0);
   if (n <= 0) return;
-  const float px = fmaf((float)gx, a.psx, a.topleft[0]);
-  const float py = fmaf((float)gy, a.psy, a.topleft[1]);
+  const float px = fmaf((float)gx, ctx.psx, ctx.topleft[0]);
+  const float py = fmaf((float)gy, ctx.psy, ctx.topleft[1]);
   float2 Y2[Sh<C>::NY2];
   float *Ws = s_w + warp * 16 * kWStride;
   float *Ys = s_y + warp * 32 * kYStride;
   int *slots = s_slots + warp * 8;
   {
     float Y[CC];
-    sh_basis<C>(a.c2w, px, py, Y);
+    sh_basis<C>(ctx.c2w, px, py, Y);
     pack_basis<C>(Y, Y2);
 #pragma unroll
     for (int k = 0; k < 16; ++k) Ys[lane * kYStride + k] = k < CC ? Y[k < CC ? k : 0] : 0.0f;
   }
   float fin[3] = {0.0f, 0.0f, 0.0f}, go[3] = {0.0f, 0.0f, 0.0f};
   if (inside) {
-    const int64_t pix = 3 * ((int64_t)gy * a.width + gx);
+    const int64_t pix = 3 * ((int64_t)gy * ctx.width + gx);
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
-      fin[ch] = a.final_img[pix + ch];
-      go[ch] = a.grad_out[pix + ch];
+      fin[ch] = ctx.final_img[pix + ch];
+      go[ch] = ctx.grad_out[pix + ch];
     }
   }
   float o[3] = {0.0f, 0.0f, 0.0f};
@@ -513,14 +591,15 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
   const float thr = a.T_thresh;
   bool done = !inside;
   float tx0, tx1, ty0, ty1;
-  tile_bounds(a, tile, tx0, tx1, ty0, ty1);
+  tile_bounds(ctx, tx0, tx1, ty0, ty1);
 
   for (int base = 0; base < n; base += B) {
     if (__syncthreads_and(done)) break;
     const int nb = min(B, n - base);
     for (int f = t; f < nb * NV; f += nthr) s_grad[f] = 0.0f;
     for (int j = t; j < nb; j += nthr) s_touched[j] = 0;
-    const int nk = load_batch<C>(a, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1, s_wcount);
+    const int nk =
+        load_batch<C>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1, s_wcount);
 
     int nslot = 0;  // warp-uniform: Gaussians staged in this warp's weight matrix
     for (int i = 0; i < nk; ++i) {
@@ -623,7 +702,7 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
         atomicAdd(a.g_alpha + id, val);
       } else {
         const int e = idx - 6, ch = e / CC, k = e - ch * CC;
-        atomicAdd(a.g_sh + (id * 3 + ch) * a.sh_stride + k, val);
+        atomicAdd(ctx.g_sh + ((id - ctx.item_lo) * 3 + ch) * ctx.sh_stride + k, val);
       }
     }
   }
@@ -644,68 +723,103 @@ size_t bwd_smem(int B, int nthr) {
 
 inline int block_threads(const RasterArgs &a) { return (a.tile_w * a.tile_h + 31) / 32 * 32; }
 
-template <int C, int MAXT>
-int launch_fwd_tt(RasterArgs a, cudaStream_t s) {
+// cudaFuncSetAttribute only when a kernel needs more dynamic shared memory
+// than it was last given (it is not a stream operation, but costs host time
+// per call).  `done` must be private to one kernel: each launcher
+// instantiation below owns its own.
+template <typename K>
+cudaError_t ensure_smem(K kernel, size_t smem, size_t &done) {
+  if (smem <= done) return cudaSuccess;
+  cudaError_t e =
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) done = smem;
+  return e;
+}
+
+template <int C, int MAXT, bool BATCHED>
+int launch_fwd_tt(RasterArgs a, int64_t grid, cudaStream_t s) {
   const int nthr = block_threads(a);
   a.batch = nthr < 128 ? nthr : 128;
   const size_t smem = fwd_smem<C>(a.batch);
-  cudaError_t e = cudaFuncSetAttribute(raster_forward_kernel<C, MAXT>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  static size_t attr_done = 0;
+  cudaError_t e = ensure_smem(raster_forward_kernel<C, MAXT, BATCHED>, smem, attr_done);
   if (e != cudaSuccess) return cuda_status(e, "raster_forward smem attribute");
-  const unsigned grid = (unsigned)(a.n_tiles_w * a.n_tiles_h);
   count_launches(1);
-  raster_forward_kernel<C, MAXT><<<grid, nthr, smem, s>>>(a);
+  raster_forward_kernel<C, MAXT, BATCHED><<<(unsigned)grid, nthr, smem, s>>>(a);
   return cuda_status(cudaGetLastError(), "raster_forward_kernel launch");
 }
 
-template <int C>
-int launch_fwd_t(const RasterArgs &a, cudaStream_t s) {
-  return block_threads(a) <= 256 ? launch_fwd_tt<C, 256>(a, s) : launch_fwd_tt<C, 1024>(a, s);
+template <int C, bool BATCHED>
+int launch_fwd_t(const RasterArgs &a, int64_t grid, cudaStream_t s) {
+  return block_threads(a) <= 256 ? launch_fwd_tt<C, 256, BATCHED>(a, grid, s)
+                                 : launch_fwd_tt<C, 1024, BATCHED>(a, grid, s);
 }
 
-template <int C, int MAXT>
-int launch_bwd_tt(RasterArgs a, cudaStream_t s) {
+template <int C, int MAXT, bool BATCHED>
+int launch_bwd_tt(RasterArgs a, int64_t grid, cudaStream_t s) {
   const int nthr = block_threads(a);
   a.batch = nthr < 64 ? nthr : 64;
   const size_t smem = bwd_smem<C>(a.batch, nthr);
-  cudaError_t e = cudaFuncSetAttribute(raster_backward_kernel<C, MAXT>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  static size_t attr_done = 0;
+  cudaError_t e = ensure_smem(raster_backward_kernel<C, MAXT, BATCHED>, smem, attr_done);
   if (e != cudaSuccess) return cuda_status(e, "raster_backward smem attribute");
-  const unsigned grid = (unsigned)(a.n_tiles_w * a.n_tiles_h);
   count_launches(1);
-  raster_backward_kernel<C, MAXT><<<grid, nthr, smem, s>>>(a);
+  raster_backward_kernel<C, MAXT, BATCHED><<<(unsigned)grid, nthr, smem, s>>>(a);
   return cuda_status(cudaGetLastError(), "raster_backward_kernel launch");
 }
 
-template <int C>
-int launch_bwd_t(const RasterArgs &a, cudaStream_t s) {
-  return block_threads(a) <= 256 ? launch_bwd_tt<C, 256>(a, s) : launch_bwd_tt<C, 1024>(a, s);
+template <int C, bool BATCHED>
+int launch_bwd_t(const RasterArgs &a, int64_t grid, cudaStream_t s) {
+  return block_threads(a) <= 256 ? launch_bwd_tt<C, 256, BATCHED>(a, grid, s)
+                                 : launch_bwd_tt<C, 1024, BATCHED>(a, grid, s);
+}
+
+template <bool BATCHED>
+int dispatch_fwd(const RasterArgs &a, int C, int64_t grid, cudaStream_t s) {
+  switch (C) {
+    case 1: return launch_fwd_t<1, BATCHED>(a, grid, s);
+    case 2: return launch_fwd_t<2, BATCHED>(a, grid, s);
+    case 3: return launch_fwd_t<3, BATCHED>(a, grid, s);
+    case 4: return launch_fwd_t<4, BATCHED>(a, grid, s);
+  }
+  set_error("SH order C must be 1..4 (got %d)", C);
+  return GSX_ERR_INVALID_ARG;
+}
+
+template <bool BATCHED>
+int dispatch_bwd(const RasterArgs &a, int C, int64_t grid, cudaStream_t s) {
+  switch (C) {
+    case 1: return launch_bwd_t<1, BATCHED>(a, grid, s);
+    case 2: return launch_bwd_t<2, BATCHED>(a, grid, s);
+    case 3: return launch_bwd_t<3, BATCHED>(a, grid, s);
+    case 4: return launch_bwd_t<4, BATCHED>(a, grid, s);
+  }
+  set_error("SH order C must be 1..4 (got %d)", C);
+  return GSX_ERR_INVALID_ARG;
 }
 
 }  // namespace
 
 int launch_raster_forward(const RasterArgs &a, int C, cudaStream_t s) {
-  if ((int64_t)a.n_tiles_w * a.n_tiles_h == 0) return GSX_OK;
-  switch (C) {
-    case 1: return launch_fwd_t<1>(a, s);
-    case 2: return launch_fwd_t<2>(a, s);
-    case 3: return launch_fwd_t<3>(a, s);
-    case 4: return launch_fwd_t<4>(a, s);
-  }
-  set_error("SH order C must be 1..4 (got %d)", C);
-  return GSX_ERR_INVALID_ARG;
+  const int64_t grid = (int64_t)a.n_tiles_w * a.n_tiles_h;
+  if (grid == 0) return GSX_OK;
+  return dispatch_fwd<false>(a, C, grid, s);
 }
 
 int launch_raster_backward(const RasterArgs &a, int C, cudaStream_t s) {
-  if ((int64_t)a.n_tiles_w * a.n_tiles_h == 0) return GSX_OK;
-  switch (C) {
-    case 1: return launch_bwd_t<1>(a, s);
-    case 2: return launch_bwd_t<2>(a, s);
-    case 3: return launch_bwd_t<3>(a, s);
-    case 4: return launch_bwd_t<4>(a, s);
-  }
-  set_error("SH order C must be 1..4 (got %d)", C);
-  return GSX_ERR_INVALID_ARG;
+  const int64_t grid = (int64_t)a.n_tiles_w * a.n_tiles_h;
+  if (grid == 0) return GSX_OK;
+  return dispatch_bwd<false>(a, C, grid, s);
+}
+
+int launch_raster_forward_batch(const RasterArgs &a, int C, int64_t total_tiles, cudaStream_t s) {
+  if (total_tiles == 0) return GSX_OK;
+  return dispatch_fwd<true>(a, C, total_tiles, s);
+}
+
+int launch_raster_backward_batch(const RasterArgs &a, int C, int64_t total_tiles, cudaStream_t s) {
+  if (total_tiles == 0) return GSX_OK;
+  return dispatch_bwd<true>(a, C, total_tiles, s);
 }
 
 }  // namespace gsx

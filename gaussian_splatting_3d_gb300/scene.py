@@ -132,6 +132,24 @@ def headline_workload(seed: int = 0, n: int = 1_000_000, width: int = 1920, heig
     return Workload("headline", scene, [view], W)
 
 
+def batch_workload(seed: int = 0, n: int = 500_000, n_views: int = 32, radius: float = 6.0,
+                   fov: float = 60.0, sizes=((800, 800), (1280, 720), (1920, 1080))) -> Workload:
+    """Multi-view batching workload: Gaussians drawn as in ``small`` (means
+    U[-1,1]^3, log-scales N(-3, 0.5), opacity logits N(0,1), DC from RGB
+    U[0,1]) with SH degree 3 (higher bands N(0, 0.05)); n_views cameras
+    uniform on the radius-6 sphere looking at the origin, image sizes cycling
+    through `sizes`.  grad_weight is None: each view's dL/dimage is drawn by
+    the caller."""
+    scene = make_scene(n, seed, mean_dist="uniform", log_scale_mu=-3.0, log_scale_sigma=0.5,
+                       alpha_sigma=1.0, sh_degree=3, dc_from_rgb=True)
+    dirs = sphere_direction(seed, 10, n_views)
+    views = []
+    for i in range(n_views):
+        w, h = sizes[i % len(sizes)]
+        views.append(View(look_at_c2w(radius * dirs[i]), CameraInfo.from_vertical_fov(fov, w, h), 16))
+    return Workload("batch", scene, views, None)
+
+
 def custom_workload(n: int, width: int, height: int, sh_degree: int, seed: int = 0,
                     radius: float = 4.0, fov: float = 60.0, tile: int = 16,
                     log_scale_mu: float = -3.0) -> Workload:

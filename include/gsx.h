@@ -153,6 +153,68 @@ typedef struct gsx_camera {
 } gsx_camera;
 
 /*
+ * One view of a batched pass.  The views of a batch are described by an
+ * array of these in device memory (plus the same array on the host for sizes).
+ * Each view names its scene (which may be shared with other views), its
+ * camera and image, where its (view, Gaussian) items start in the per-item
+ * arrays and where its tiles start in the global tile numbering.
+ */
+typedef struct gsx_batch_view {
+  const float *mean, *qvec, *log_scale, *alpha_logit, *sh; /* the view's scene */
+  float *g_mean, *g_qvec, *g_log_scale, *g_alpha_logit;    /* scene gradients (backward) */
+  float *g_sh;                                             /* SH gradient [n,3,sh_stride] */
+  int64_t n_gaussians;  /* Gaussians in the scene */
+  int64_t item_offset;  /* first item of this view: items are (view, Gaussian) pairs */
+  int64_t tile_offset;  /* first global tile of this view */
+  int32_t sh_stride, sh_order;
+  int32_t tile_w, tile_h, n_tiles_w, n_tiles_h;
+  float topleft[2];
+  float pixel_size_x, pixel_size_y;
+  float *out;            /* [height, width, 3] */
+  const float *grad_out; /* dL/dout [height, width, 3] (backward) */
+  int32_t write_empty_tiles, reserved;
+  gsx_camera cam;
+} gsx_batch_view;
+
+/* sizeof(gsx_batch_view), for bindings that build the table themselves. */
+size_t gsx_batch_view_size(void);
+
+/*
+ * Batched passes over n_views views (table in device memory, views_dev, and
+ * the same table on the host, views_host).  Per-item arrays (mean2d f32[I,2],
+ * cov2d f32[I,4], depth f32[I], alpha f32[I], rect i32[I,4], counts i32[I],
+ * g_mean2d, g_cov2d, g_alpha) have I = sum of the views' n_gaussians entries;
+ * start/end have one entry per tile of the batch (sum of the views' tiles).
+ * All views share the tile shape and the SH order.  The binning is
+ * asynchronous (read its key count with gsx_binning_status using I as the
+ * Gaussian count).  gsx_batch_project_backward needs all views to share one
+ * scene and writes that scene's gradients (views[0].g_*), summed over views;
+ * the raster backward adds SH gradients into each view's g_sh.
+ */
+int gsx_batch_project_forward(const gsx_batch_view *views_dev, const gsx_batch_view *views_host,
+                              int32_t n_views, float frustum_radius, float tile_radius,
+                              float *mean2d, float *cov2d, float *depth, float *alpha,
+                              int32_t *rect, int32_t *counts, void *stream);
+int gsx_batch_bin_async(const gsx_batch_view *views_dev, const gsx_batch_view *views_host,
+                        int32_t n_views, const int32_t *rect, const int32_t *counts,
+                        const float *depth, int64_t key_capacity, int32_t *gaussian_ids,
+                        int32_t *start, int32_t *end, void *workspace, size_t workspace_bytes,
+                        void *stream);
+int gsx_batch_render_forward(const gsx_batch_view *views_dev, const gsx_batch_view *views_host,
+                             int32_t n_views, int64_t key_capacity, const float *mean2d,
+                             const float *cov2d, const float *alpha, const int32_t *start,
+                             const int32_t *end, const int32_t *gaussian_ids, float T_thresh,
+                             void *stream);
+int gsx_batch_render_backward(const gsx_batch_view *views_dev, const gsx_batch_view *views_host,
+                              int32_t n_views, int64_t key_capacity, const float *mean2d,
+                              const float *cov2d, const float *alpha, const int32_t *start,
+                              const int32_t *end, const int32_t *gaussian_ids, float *g_mean2d,
+                              float *g_cov2d, float *g_alpha, float T_thresh, void *stream);
+int gsx_batch_project_backward(const gsx_batch_view *views_dev, const gsx_batch_view *views_host,
+                               int32_t n_views, const int32_t *counts, const float *g_mean2d,
+                               const float *g_cov2d, const float *g_alpha, void *stream);
+
+/*
  * One pass over n Gaussians (mean f32[n,3], qvec f32[n,4] WXYZ,
  * log_scale f32[n,3], alpha_logit f32[n]): scale = exp(log_scale),
  * alpha = sigmoid(alpha_logit), bounding-sphere cull (radius factor
