@@ -401,16 +401,122 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def run_serve(args):
+    """Served views/s with p50/p99 latency for the serving workload: 8 resident
+    scenes, a Poisson request stream fed at its arrival times, forward only,
+    admission against a 150 GB budget, continuous batching on two streams.
+    Also: capacity (all requests queued at once), plain per-view launches of
+    the same requests, and served-vs-alone image identity."""
+    import torch
+
+    from gaussian_splatting_3d_gb300 import _lib, renderer, serve
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    scenes = serve.serving_scenes(dev)
+    arrivals = serve.poisson_requests(len(scenes), args.rate, args.duration, seed=1)
+    st = renderer.RasterSettings()
+
+    def server(**kw):
+        return serve.RenderServer(scenes, dev, budget_bytes=args.budget_gb * 1e9, max_views=args.max_views,
+                                  slots=args.slots, settings=st, **kw)
+
+    # warm-up: kernels, allocator, keys-per-Gaussian estimates
+    warm = server(retain_images=False)
+    serve.run_stream(warm, arrivals[:min(len(arrivals), 64 * args.warmup)], realtime=False)
+    kpg = dict(warm.keys_per_gaussian)
+
+    # the stream at its arrival times
+    srv = server(retain_images=False)
+    srv.keys_per_gaussian = dict(kpg)
+    clocks = ClockSampler(0)
+    torch.cuda.synchronize()
+    torch.cuda.reset_peak_memory_stats(dev)
+    launches0 = _lib.load().gsx_kernel_launch_count()
+    clocks.start()
+    reqs, wall = serve.run_stream(srv, arrivals, realtime=True)
+    clock_info = clocks.stop()
+    launches = int(_lib.load().gsx_kernel_launch_count() - launches0)
+    peak_hbm = torch.cuda.max_memory_allocated(dev)
+    lat = serve.latency_stats(reqs)
+    done = sum(r.state == "done" for r in reqs)
+
+    # capacity: the first requests all queued at once
+    n_cap = min(len(arrivals), args.capacity_requests)
+    cap_srv = server(retain_images=False)
+    cap_srv.keys_per_gaussian = dict(kpg)
+    _, cap_wall = serve.run_stream(cap_srv, arrivals[:n_cap], realtime=False)
+
+    # plain per-view launches of the same requests, one after another
+    n_plain = min(len(arrivals), args.plain_requests)
+    pipe = renderer.ViewPipeline(dev)
+
+    def plain(a):
+        sc = scenes[a[1]]
+        return pipe.forward(sc.mean, sc.qvec, sc.log_scale, sc.sh, sc.alpha_logit, a[2], a[3], st)["out"]
+
+    for a in arrivals[:8]:
+        plain(a)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for a in arrivals[:n_plain]:
+        plain(a)
+    torch.cuda.synchronize()
+    plain_wall = time.perf_counter() - t0
+
+    # served in a mix vs rendered alone: the same bits
+    chk = server()
+    chk.keys_per_gaussian = dict(kpg)
+    mixed, _ = serve.run_stream(chk, arrivals[:24], realtime=False)
+    same = all(torch.equal(r.image, plain(a)) for r, a in zip(mixed, arrivals[:24]))
+
+    sizes = np.array(srv.batch_sizes)
+    line = {
+        "metric": f"served views/s (Poisson {args.rate:g} req/s for {args.duration:g} s, 8 scenes, forward)",
+        "value": round(done / wall, 2), "unit": "views/s", "higher_is_better": True,
+        "n_gpus": 1, "steps": len(reqs), "warmup": args.warmup,
+        "ms_per_step": round(wall * 1e3 / max(1, done), 4),
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (8 seeded scenes, Poisson arrivals; no dataset)",
+        "p50_ms": round(lat["p50_ms"], 3), "p99_ms": round(lat["p99_ms"], 3),
+        "mean_ms": round(lat["mean_ms"], 3), "max_ms": round(lat["max_ms"], 3),
+        "requests": len(reqs), "served": int(done), "batches": srv.n_batches,
+        "mean_batch": round(float(sizes.mean()), 2) if sizes.size else 0.0,
+        "reruns": srv.n_reruns, "key_margin": srv.margin,
+        "host_ms_per_batch": round(srv.host_launch_s * 1e3 / max(1, srv.n_batches), 3),
+        "capacity_views_per_s": round(n_cap / cap_wall, 2),
+        "plain_per_view_views_per_s": round(n_plain / plain_wall, 2),
+        "capacity_vs_plain": round((n_cap / cap_wall) / (n_plain / plain_wall), 3),
+        "identical_to_alone": bool(same),
+        "peak_reserved_gb": round(srv.peak_reserved / 1e9, 3),
+        "peak_hbm_gb": round(peak_hbm / 1e9, 3),
+        "scene_sizes": [s.n for s in scenes],
+        "gpu_launches": launches, "clocks": clock_info,
+        "config": {"workload": "serve: 8 resident scenes (log-uniform 100k-2M Gaussians, SH degree 0), "
+                               "Poisson arrivals, sizes 512x512/1280x720/1920x1080, 16x16 tiles",
+                   "budget_gb": args.budget_gb, "max_views": args.max_views, "slots": args.slots,
+                   "rate": args.rate, "duration_s": args.duration},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gsx", choices=["gsx", "reference"])
-    ap.add_argument("--workload", default="headline", choices=["headline", "small", "batch"])
+    ap.add_argument("--workload", default="headline", choices=["headline", "small", "batch", "serve"])
     ap.add_argument("--views", type=int, default=32)
     ap.add_argument("--n-batch", type=int, default=500_000)
     ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--rate", type=float, default=2000.0, help="serve: request arrivals per second")
+    ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
+    ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--max-views", type=int, default=16)
+    ap.add_argument("--slots", type=int, default=2)
+    ap.add_argument("--capacity-requests", type=int, default=4000)
+    ap.add_argument("--plain-requests", type=int, default=1000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-frac", type=float, default=1.0 / 8.0)
     args = ap.parse_args()
@@ -420,6 +526,8 @@ def main():
         run_reference(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "serve":
+        run_serve(args)
     else:
         run_gsx(args)
 

@@ -105,6 +105,8 @@ SIGNATURES = {
         [c_int64, P, P, P, c_int32, c_int32, c_int64, P, P, P, P, c_size_t, P],
     ),
     "gsx_binning_status": (c_int, [P, c_int64, c_int64, c_int32, c_int32, POINTER(c_int64), P]),
+    "gsx_binning_status_copy_async": (c_int, [P, c_int64, c_int64, P, P]),
+    "gsx_binning_status_decode": (c_int, [P, c_int64, c_int32, c_int32, POINTER(c_int64)]),
     "gsx_render_forward": (
         c_int,
         [POINTER(GsxRasterParams), c_int64, c_int64, P, P, P, P, P, P, P, P, P, P, P],

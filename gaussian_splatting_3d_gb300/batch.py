@@ -155,8 +155,9 @@ class BatchPipeline:
             tile += ntw * nth
         self.n_items, self.n_tiles = item, tile
         self.table = table
-        raw = np.frombuffer(bytes(table), dtype=np.uint8)
-        self.table_dev = torch.from_numpy(raw.copy()).to(dev)
+        raw = torch.frombuffer(bytearray(bytes(table)), dtype=torch.uint8)
+        self._table_pinned = raw.pin_memory()  # kept alive until the copy has run
+        self.table_dev = self._table_pinned.to(dev, non_blocking=True)
         I = item
         f32 = dict(dtype=torch.float32, device=dev)
         self.mean2d = torch.empty((I, 2), **f32)
@@ -171,7 +172,8 @@ class BatchPipeline:
             self.g_mean2d = torch.zeros((I, 2), **f32)
             self.g_cov2d = torch.zeros((I, 4), **f32)
             self.g_alpha = torch.zeros((I,), **f32)
-        self._alloc_keys(max(self.key_capacity, 4 * I, 1 << 16))
+        # a capacity set before planning is kept (callers that size it themselves)
+        self._alloc_keys(self.key_capacity if self.key_capacity > 0 else max(4 * I, 1 << 16))
         self.graph = None
         return self
 

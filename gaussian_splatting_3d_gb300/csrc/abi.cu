@@ -161,6 +161,25 @@ int gsx_binning_status(const void *workspace, int64_t n_gaussians, int64_t key_c
                         nullptr, as_stream(stream));
 }
 
+int gsx_binning_status_copy_async(const void *workspace, int64_t n_gaussians,
+                                  int64_t key_capacity, void *dst, void *stream) {
+  g_err[0] = 0;
+  GSX_REQUIRE(workspace && dst, "null pointer argument");
+  GSX_REQUIRE(n_gaussians >= 0 && key_capacity >= 0, "negative size");
+  return copy_binning_status_async(workspace, n_gaussians, key_capacity, dst, as_stream(stream));
+}
+
+int gsx_binning_status_decode(const void *block, int64_t key_capacity, int32_t n_tiles_w,
+                              int32_t n_tiles_h, int64_t *n_keys_out) {
+  g_err[0] = 0;
+  GSX_REQUIRE(block, "null status block");
+  uint64_t w[2];
+  std::memcpy(w, block, sizeof(w));
+  if (n_keys_out) *n_keys_out = (int64_t)w[0];
+  return decode_binning_status(w[0], (uint32_t)(w[1] & 0xffffffffu), key_capacity, n_tiles_w,
+                               n_tiles_h);
+}
+
 static int check_raster(const RasterArgs &a, int C, int64_t n, int64_t n_keys) {
   GSX_REQUIRE(C >= 1 && C <= 4, "SH order C must be 1..4 (got %d)", C);
   GSX_REQUIRE(a.tile_w > 0 && a.tile_h > 0 && a.tile_w * a.tile_h <= 1024,

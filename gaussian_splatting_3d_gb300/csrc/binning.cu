@@ -47,6 +47,7 @@ constexpr uint32_t kErrTimeout = 1u;
 constexpr uint32_t kErrCount = 2u;
 constexpr uint32_t kErrRange = 4u;  // rectangle outside the tile grid
 constexpr uint32_t kErrIndex = 8u;  // corrupted depth order (after a timeout)
+constexpr size_t kStatusBlockBytes = 16;
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
   uint32_t m;
@@ -398,9 +399,12 @@ Workspace carve_ws(void *base, int64_t n, int64_t cap) {
   w.emit_words = (nn + kEmitTile - 1) / kEmitTile;
   w.emit_status = reinterpret_cast<unsigned long long *>(take(8 * w.emit_words));
   w.counters = reinterpret_cast<uint32_t *>(take(16 * 4));
-  w.error = reinterpret_cast<uint32_t *>(take(4));
-  w.total = reinterpret_cast<unsigned long long *>(take(8));
-  w.k_eff = reinterpret_cast<uint32_t *>(take(4));
+  // the status block: key total (u64), error bits (u32), key count used (u32),
+  // 16 contiguous bytes that one copy brings back
+  char *status_block = take(kStatusBlockBytes);
+  w.total = reinterpret_cast<unsigned long long *>(status_block);
+  w.error = reinterpret_cast<uint32_t *>(status_block ? status_block + 8 : nullptr);
+  w.k_eff = reinterpret_cast<uint32_t *>(status_block ? status_block + 12 : nullptr);
   w.bytes = off;
   return w;
 }
@@ -473,9 +477,7 @@ int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
   cudaError_t e = cudaMemsetAsync(start, 0xff, sizeof(int32_t) * (size_t)n_tiles, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(end, 0xff, sizeof(int32_t) * (size_t)n_tiles, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(w.counters, 0, 16 * 4, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(w.error, 0, 4, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(w.total, 0, 8, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(w.k_eff, 0, 4, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.total, 0, kStatusBlockBytes, s);
   if (e != cudaSuccess) return cuda_status(e, "memset binning state");
   if (n == 0) return GSX_OK;
   const uint32_t nn = (uint32_t)n;
@@ -526,20 +528,9 @@ int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
   return GSX_OK;
 }
 
-// Read the key total and error bits left by run_binning_async (synchronises
-// `s`) and turn them into a status.
-int binning_status(const void *ws, int64_t n, int64_t capacity, int32_t n_tiles_w,
-                   int32_t n_tiles_h, int64_t *n_keys_host, uint32_t *flags_host,
-                   cudaStream_t s) {
-  Workspace w = carve_ws(const_cast<void *>(ws), n, capacity);
-  unsigned long long total_h = 0;
-  uint32_t err_h = 0;
-  cudaError_t e = cudaMemcpyAsync(&total_h, w.total, 8, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&err_h, w.error, 4, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return cuda_status(e, "read binning status");
-  if (n_keys_host) *n_keys_host = (int64_t)total_h;
-  if (flags_host) *flags_host = err_h;
+// Turn a copied status block (key total, error bits) into a status.
+int decode_binning_status(unsigned long long total_h, uint32_t err_h, int64_t capacity,
+                          int32_t n_tiles_w, int32_t n_tiles_h) {
   if (err_h & kErrTimeout) {
     set_error("binning: a look-back wait expired");
     return GSX_ERR_TIMEOUT;
@@ -561,6 +552,32 @@ int binning_status(const void *ws, int64_t n, int64_t capacity, int32_t n_tiles_
     return GSX_ERR_CAPACITY;
   }
   return GSX_OK;
+}
+
+// Enqueue a copy of the status block left by run_binning_async into dst
+// (16 bytes of pinned host or device memory); no synchronisation.
+int copy_binning_status_async(const void *ws, int64_t n, int64_t capacity, void *dst,
+                              cudaStream_t s) {
+  Workspace w = carve_ws(const_cast<void *>(ws), n, capacity);
+  cudaError_t e = cudaMemcpyAsync(dst, w.total, kStatusBlockBytes, cudaMemcpyDefault, s);
+  return e == cudaSuccess ? GSX_OK : cuda_status(e, "copy binning status");
+}
+
+// Read the key total and error bits left by run_binning_async (synchronises
+// `s`) and turn them into a status.
+int binning_status(const void *ws, int64_t n, int64_t capacity, int32_t n_tiles_w,
+                   int32_t n_tiles_h, int64_t *n_keys_host, uint32_t *flags_host,
+                   cudaStream_t s) {
+  Workspace w = carve_ws(const_cast<void *>(ws), n, capacity);
+  uint64_t block[2] = {0, 0};
+  cudaError_t e = cudaMemcpyAsync(block, w.total, kStatusBlockBytes, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_status(e, "read binning status");
+  const unsigned long long total_h = block[0];
+  const uint32_t err_h = (uint32_t)(block[1] & 0xffffffffu);
+  if (n_keys_host) *n_keys_host = (int64_t)total_h;
+  if (flags_host) *flags_host = err_h;
+  return decode_binning_status(total_h, err_h, capacity, n_tiles_w, n_tiles_h);
 }
 
 int run_binning(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,

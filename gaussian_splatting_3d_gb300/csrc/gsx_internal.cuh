@@ -130,6 +130,10 @@ int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
                       int64_t total_tiles = 0);
 int binning_status(const void *ws, int64_t n, int64_t capacity, int32_t n_tiles_w,
                    int32_t n_tiles_h, int64_t *n_keys_host, uint32_t *flags_host, cudaStream_t s);
+int copy_binning_status_async(const void *ws, int64_t n, int64_t capacity, void *dst,
+                              cudaStream_t s);
+int decode_binning_status(unsigned long long total, uint32_t error_bits, int64_t capacity,
+                          int32_t n_tiles_w, int32_t n_tiles_h);
 int run_binning(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
                 int32_t rect_stride, const int32_t *counts, const float *depth,
                 int32_t n_tiles_w, int32_t n_tiles_h, int64_t capacity,

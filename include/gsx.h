@@ -266,6 +266,20 @@ int gsx_binning_status(const void *workspace, int64_t n_gaussians, int64_t key_c
                        int32_t n_tiles_w, int32_t n_tiles_h, int64_t *n_keys_out,
                        void *stream);
 
+/*
+ * Non-blocking form of gsx_binning_status, for callers that keep several
+ * binnings in flight (no reference counterpart: the reference's binning
+ * always synchronises).  gsx_binning_status_copy_async enqueues on `stream`
+ * a copy of the binning's 16-byte status block (u64 key total, u32 error
+ * bits, u32 key count used) into dst (pinned host or device memory);
+ * gsx_binning_status_decode turns a block that has arrived into the status
+ * gsx_binning_status would return, and the key total.
+ */
+int gsx_binning_status_copy_async(const void *workspace, int64_t n_gaussians,
+                                  int64_t key_capacity, void *dst, void *stream);
+int gsx_binning_status_decode(const void *block, int64_t key_capacity, int32_t n_tiles_w,
+                              int32_t n_tiles_h, int64_t *n_keys_out);
+
 /* Raster parameters of the fused path. */
 typedef struct gsx_raster_params {
   int32_t width, height;

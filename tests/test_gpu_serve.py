@@ -1,0 +1,151 @@
+"""Continuous-batching render server.
+
+* every served image is bit-identical to rendering the same request alone
+  (single-view path, same tile shape), whatever batch it landed in and
+  whatever ran beside it on the other stream;
+* admission keeps the reserved bytes within the budget and still serves
+  everything; a request larger than the whole budget is rejected up front;
+* an under-estimated key capacity is detected from the asynchronously copied
+  status block and the batch is re-run before its images are published;
+* waiting requests can be cancelled and are never rendered.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from gaussian_splatting_3d_gb300 import batch as B  # noqa: E402
+from gaussian_splatting_3d_gb300 import renderer, scene as S, serve  # noqa: E402
+from gaussian_splatting_3d_gb300.camera import CameraInfo, look_at_c2w  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+SIZES = ((96, 80), (128, 96), (64, 64), (160, 90))
+
+
+def dev():
+    return torch.device("cuda:0")
+
+
+def make_scenes(degrees=(3, 3, 3), counts=(1500, 4000, 2500), seed=70):
+    out = []
+    for i, (n, d) in enumerate(zip(counts, degrees)):
+        out.append(B.Scene.from_arrays(S.custom_workload(n, 64, 64, d, seed=seed + i).scene, dev()))
+    return out
+
+
+def make_requests(n, n_scenes, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        w, h = SIZES[i % len(SIZES)]
+        out.append((int(rng.integers(n_scenes)), look_at_c2w(rng.uniform(3.5, 6.0) * d),
+                    CameraInfo.from_vertical_fov(55.0, w, h)))
+    return out
+
+
+def alone(scene, c2w, cam, settings=None):
+    return renderer.rasterize(scene.mean, scene.qvec, scene.log_scale, scene.sh, scene.alpha_logit, c2w, cam,
+                              settings or renderer.RasterSettings())
+
+
+def test_served_images_equal_alone_and_in_the_mix():
+    scenes = make_scenes()
+    srv = serve.RenderServer(scenes, dev(), max_views=5, slots=2)
+    reqs = [srv.submit(*r) for r in make_requests(23, len(scenes), seed=1)]
+    # more requests arrive while the first batches are on the GPU
+    srv.poll()
+    reqs += [srv.submit(*r) for r in make_requests(9, len(scenes), seed=2)]
+    srv.drain()
+    torch.cuda.synchronize()
+    assert all(r.state == "done" for r in reqs)
+    assert srv.n_batches >= 7 and max(srv.batch_sizes) <= 5
+    assert len({r.batch_id for r in reqs}) == srv.n_batches
+    for r in reqs:
+        ref = alone(scenes[r.scene], r.c2w, r.cam)
+        np.testing.assert_array_equal(r.image.cpu().numpy(), ref.cpu().numpy())
+    # and served alone (one view per batch, one slot): the same bits again
+    solo = serve.RenderServer(scenes, dev(), max_views=1, slots=1)
+    for r in reqs[:6]:
+        q = solo.submit(r.scene, r.c2w, r.cam)
+        solo.drain()
+        np.testing.assert_array_equal(q.image.cpu().numpy(), r.image.cpu().numpy())
+
+
+def test_mixed_sh_orders_split_into_batches():
+    scenes = make_scenes(degrees=(0, 3, 1), seed=80)
+    srv = serve.RenderServer(scenes, dev(), max_views=8)
+    reqs = [srv.submit(*r) for r in make_requests(12, len(scenes), seed=3)]
+    srv.drain()
+    torch.cuda.synchronize()
+    by_batch = {}
+    for r in reqs:
+        by_batch.setdefault(r.batch_id, set()).add(srv.sh_orders[r.scene])
+        ref = alone(scenes[r.scene], r.c2w, r.cam)
+        np.testing.assert_array_equal(r.image.cpu().numpy(), ref.cpu().numpy())
+    assert all(len(v) == 1 for v in by_batch.values())
+
+
+def test_admission_keeps_within_budget():
+    scenes = make_scenes(seed=90)
+    probe = serve.RenderServer(scenes, dev())
+    reqs_spec = make_requests(10, len(scenes), seed=4)
+    # room for about three requests at a time (batch bytes are sub-additive:
+    # the key buffer has a minimum size and the workspace fixed parts)
+    three = probe._batch_bytes([serve.Request(s, c, cam) for s, c, cam in reqs_spec[:3]])
+    budget = probe.resident + three
+    srv = serve.RenderServer(scenes, dev(), budget_bytes=budget, max_views=8, slots=2)
+    reqs = [srv.submit(*r) for r in reqs_spec]
+    srv.drain()
+    torch.cuda.synchronize()
+    assert all(r.state == "done" for r in reqs)
+    assert srv.peak_reserved <= budget - srv.resident
+    assert srv.n_batches >= 3  # unconstrained, max_views=8 takes them in two
+    for r in reqs[:4]:
+        np.testing.assert_array_equal(r.image.cpu().numpy(), alone(scenes[r.scene], r.c2w, r.cam).cpu().numpy())
+    big = serve.RenderServer(scenes, dev(), budget_bytes=probe.resident + 1024)
+    q = big.submit(*reqs_spec[0])
+    assert q.state == "rejected" and big.idle
+
+
+def test_underestimated_capacity_reruns_before_publishing():
+    scenes = make_scenes(seed=100)
+    srv = serve.RenderServer(scenes, dev(), max_views=4, keys_per_gaussian=1e-3)
+    # keep the minimum capacity from hiding the under-estimate
+    serve_min = serve.MIN_KEYS
+    serve.MIN_KEYS = 16
+    try:
+        reqs = [srv.submit(*r) for r in make_requests(8, len(scenes), seed=5)]
+        srv.drain()
+    finally:
+        serve.MIN_KEYS = serve_min
+    torch.cuda.synchronize()
+    assert srv.n_reruns >= 1
+    for r in reqs:
+        np.testing.assert_array_equal(r.image.cpu().numpy(), alone(scenes[r.scene], r.c2w, r.cam).cpu().numpy())
+
+
+def test_cancel_waiting_request():
+    scenes = make_scenes(seed=110)
+    srv = serve.RenderServer(scenes, dev(), max_views=2, slots=1)
+    reqs = [srv.submit(*r) for r in make_requests(6, len(scenes), seed=6)]
+    srv.poll()  # the first batch is admitted; the rest wait
+    victim = reqs[-1]
+    assert victim.state == "waiting"
+    assert srv.cancel(victim)
+    assert not srv.cancel(reqs[0])  # already running
+    srv.drain()
+    assert victim.state == "cancelled" and victim.image is None
+    assert all(r.state == "done" for r in reqs[:-1])
+
+
+def test_poisson_stream_smoke():
+    scenes = make_scenes(seed=120)
+    arrivals = [(t, s, c, cam) for t, (s, c, cam) in zip(np.arange(16) * 2e-4, make_requests(16, len(scenes), 7))]
+    srv = serve.RenderServer(scenes, dev(), max_views=4)
+    reqs, wall = serve.run_stream(srv, arrivals, realtime=True)
+    st = serve.latency_stats(reqs)
+    assert len(reqs) == 16 and all(r.state == "done" for r in reqs)
+    assert 0 < st["p50_ms"] <= st["p99_ms"] and wall > 0
