@@ -500,13 +500,85 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+def run_memory(args):
+    """Memory-pressure workload: 3,000,000 Gaussians (headline distribution),
+    SH degree 3, one 3840x2160 view, fwd+bwd.  Times the step with the
+    projection recomputed in backward (only the tile lists held between
+    forward and backward) and with it stored, and reports peak HBM and the
+    bytes held between forward and backward for both."""
+    import torch
+
+    from gaussian_splatting_3d_gb300 import _lib, renderer, scene as S
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    wl = S.headline_workload(n=args.n_memory, width=3840, height=2160)
+    sc, view = wl.scene, wl.views[0]
+    params = [torch.from_numpy(a).to(dev) for a in (sc.mean, sc.qvec, sc.log_scale, sc.sh, sc.alpha_logit)]
+    W = torch.from_numpy(wl.grad_weight).to(dev)
+    pipe = renderer.ViewPipeline(dev)
+    out = {}
+    for mode in ("recompute", "stored"):
+        st = renderer.RasterSettings(recompute_projection=(mode == "recompute"))
+        renderer._bin_buffers(dev).release()
+
+        def step(timer=None):
+            state = pipe.forward(*params, view.c2w, view.cam, st, timer=timer)
+            held = torch.cuda.memory_allocated(dev)
+            pipe.backward(state, *params, W, timer=timer)
+            return state, held
+
+        for _ in range(args.warmup):
+            state, _ = step()
+        del state
+        torch.cuda.synchronize()
+        renderer._bin_buffers(dev).release()
+        base = torch.cuda.memory_allocated(dev)
+        torch.cuda.reset_peak_memory_stats(dev)
+        state, held = step()
+        K = state["K"]
+        del state
+        torch.cuda.synchronize()
+        peak = torch.cuda.max_memory_allocated(dev)
+        timer = renderer.StageTimer()
+        launches0 = _lib.load().gsx_kernel_launch_count()
+        clocks = ClockSampler(0)
+        clocks.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            step(timer)
+        e1.record()
+        torch.cuda.synchronize()
+        out[mode] = {"ms": e0.elapsed_time(e1) / args.steps, "peak_hbm_gb": peak / 1e9,
+                     "held_fwd_to_bwd_gb": (held - base) / 1e9, "keys": K,
+                     "stages_ms": {k: round(v["mean_ms"], 4) for k, v in timer.summary().items()},
+                     "gpu_launches": int(_lib.load().gsx_kernel_launch_count() - launches0),
+                     "clocks": clocks.stop()}
+    r = out["recompute"]
+    line = {
+        "metric": f"fwd+bwd ms/iter ({sc.n} Gaussians, 3840x2160, projection recomputed in backward)",
+        "value": round(r["ms"], 4), "unit": "ms/iter", "higher_is_better": False,
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(r["ms"], 4),
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded PCG64 scene of the headline distribution; no dataset)",
+        "peak_hbm_gb": round(r["peak_hbm_gb"], 3), "held_fwd_to_bwd_gb": round(r["held_fwd_to_bwd_gb"], 3),
+        "keys": r["keys"], "stages_ms": r["stages_ms"], "gpu_launches": r["gpu_launches"], "clocks": r["clocks"],
+        "stored_projection": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in out["stored"].items()
+                              if k in ("ms", "peak_hbm_gb", "held_fwd_to_bwd_gb")},
+        "config": {"workload": f"memory: {sc.n} Gaussians, SH degree 3, 3840x2160, 16x16 tiles, fwd+bwd",
+                   "params_gb": round(sum(p.numel() * 4 for p in params) / 1e9, 3)},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gsx", choices=["gsx", "reference"])
-    ap.add_argument("--workload", default="headline", choices=["headline", "small", "batch", "serve"])
+    ap.add_argument("--workload", default="headline", choices=["headline", "small", "batch", "serve", "memory"])
     ap.add_argument("--views", type=int, default=32)
     ap.add_argument("--n-batch", type=int, default=500_000)
     ap.add_argument("--n", type=int, default=1_000_000)
@@ -517,6 +589,7 @@ def main():
     ap.add_argument("--slots", type=int, default=2)
     ap.add_argument("--capacity-requests", type=int, default=4000)
     ap.add_argument("--plain-requests", type=int, default=1000)
+    ap.add_argument("--n-memory", type=int, default=3_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-frac", type=float, default=1.0 / 8.0)
     args = ap.parse_args()
@@ -528,6 +601,8 @@ def main():
         run_batch(args)
     elif args.workload == "serve":
         run_serve(args)
+    elif args.workload == "memory":
+        run_memory(args)
     else:
         run_gsx(args)
 

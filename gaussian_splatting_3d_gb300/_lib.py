@@ -11,12 +11,16 @@ from ctypes import POINTER, c_char_p, c_float, c_int, c_int32, c_int64, c_size_t
 
 from . import _build
 
+GSX_ABI_VERSION = 2  # include/gsx.h
 GSX_OK = 0
 GSX_ERR_INVALID_ARG = 1
 GSX_ERR_CAPACITY = 2
 GSX_ERR_TIMEOUT = 3
 GSX_ERR_CUDA = 4
 GSX_ERR_MISMATCH = 5
+# gradient flags of the projection backward (include/gsx.h)
+GSX_GRAD_DEPTH, GSX_GRAD_JACOBIAN, GSX_GRAD_CLAMP = 1, 2, 4
+GSX_GRAD_EXACT = 7
 
 
 class GsxError(RuntimeError):
@@ -117,7 +121,7 @@ SIGNATURES = {
     ),
     "gsx_project_backward": (
         c_int,
-        [c_int64, P, P, P, P, POINTER(GsxCamera), P, P, P, P, P, P, P, P, P],
+        [c_int64, P, P, P, P, POINTER(GsxCamera), P, P, P, P, P, P, P, P, c_int32, P],
     ),
     # batched passes (views_dev, views_host, n_views, ...)
     "gsx_batch_view_size": (c_size_t, []),
@@ -125,7 +129,7 @@ SIGNATURES = {
     "gsx_batch_bin_async": (c_int, [P, P, c_int32, P, P, P, c_int64, P, P, P, P, c_size_t, P]),
     "gsx_batch_render_forward": (c_int, [P, P, c_int32, c_int64] + [P] * 6 + [c_float, P]),
     "gsx_batch_render_backward": (c_int, [P, P, c_int32, c_int64] + [P] * 9 + [c_float, P]),
-    "gsx_batch_project_backward": (c_int, [P, P, c_int32] + [P] * 4 + [P]),
+    "gsx_batch_project_backward": (c_int, [P, P, c_int32] + [P] * 4 + [c_int32, P]),
 }
 
 _lib = None
@@ -156,6 +160,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
+        if lib.gsx_abi_version() != GSX_ABI_VERSION:
+            raise ImportError(f"{_build.LIB_PATH} has ABI version {lib.gsx_abi_version()}, the bindings expect "
+                              f"{GSX_ABI_VERSION}: rebuild it")
         _lib = lib
         return lib
 

@@ -218,7 +218,8 @@ class BatchPipeline:
                                                  ptr(self.g_mean2d), ptr(self.g_cov2d), ptr(self.g_alpha),
                                                  float(self.settings.T_thresh), s), "gsx_batch_render_backward")
         _lib.check(lib.gsx_batch_project_backward(vd, vh, V, ptr(self.counts), ptr(self.g_mean2d),
-                                                  ptr(self.g_cov2d), ptr(self.g_alpha), s),
+                                                  ptr(self.g_cov2d), ptr(self.g_alpha),
+                                                  self.settings.grad_flags(), s),
                    "gsx_batch_project_backward")
 
     def key_status(self):

@@ -60,7 +60,7 @@ const char *gsx_status_string(int status) {
 
 const char *gsx_last_error(void) { return g_err; }
 
-int gsx_abi_version(void) { return 1; }
+int gsx_abi_version(void) { return GSX_ABI_VERSION; }
 
 uint64_t gsx_kernel_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
@@ -378,10 +378,11 @@ int gsx_project_backward(int64_t n, const float *mean, const float *qvec,
                          const float *grad_mean2d, const float *grad_cov2d,
                          const float *grad_alpha, float *grad_mean,
                          float *grad_qvec, float *grad_log_scale,
-                         float *grad_alpha_logit, void *stream) {
+                         float *grad_alpha_logit, int32_t grad_flags, void *stream) {
   g_err[0] = 0;
   GSX_REQUIRE(n >= 0, "n must be >= 0");
   GSX_REQUIRE(cam, "null camera");
+  GSX_REQUIRE((grad_flags & ~GSX_GRAD_EXACT) == 0, "unknown grad_flags bits 0x%x", grad_flags);
   if (n == 0) return GSX_OK;
   GSX_REQUIRE(mean && qvec && log_scale && alpha_logit && counts && grad_mean2d &&
                   grad_cov2d && grad_alpha && grad_mean && grad_qvec && grad_log_scale &&
@@ -392,7 +393,7 @@ int gsx_project_backward(int64_t n, const float *mean, const float *qvec,
               "qvec, grad_qvec, grad_cov2d must be 16-byte aligned, grad_mean2d 8-byte");
   return launch_project_backward(n, mean, qvec, log_scale, alpha_logit, *cam, counts,
                                  grad_mean2d, grad_cov2d, grad_alpha, grad_mean, grad_qvec,
-                                 grad_log_scale, grad_alpha_logit, as_stream(stream));
+                                 grad_log_scale, grad_alpha_logit, grad_flags, as_stream(stream));
 }
 
 }  // extern "C"

@@ -190,7 +190,12 @@ int gsx_batch_render_backward(const gsx_batch_view *views_dev, const gsx_batch_v
 
 int gsx_batch_project_backward(const gsx_batch_view *views_dev, const gsx_batch_view *views_host,
                                int32_t n_views, const int32_t *counts, const float *g_mean2d,
-                               const float *g_cov2d, const float *g_alpha, void *stream) {
+                               const float *g_cov2d, const float *g_alpha, int32_t grad_flags,
+                               void *stream) {
+  if ((grad_flags & ~GSX_GRAD_EXACT) != 0) {
+    set_error("unknown grad_flags bits 0x%x", grad_flags);
+    return GSX_ERR_INVALID_ARG;
+  }
   BatchShape b;
   int st = check_views(views_host, n_views, b);
   if (st != GSX_OK) return st;
@@ -211,7 +216,7 @@ int gsx_batch_project_backward(const gsx_batch_view *views_dev, const gsx_batch_
     return GSX_ERR_INVALID_ARG;
   }
   return launch_project_backward_batch(views_dev, n_views, v.n_gaussians, counts, g_mean2d,
-                                       g_cov2d, g_alpha, as_stream(stream));
+                                       g_cov2d, g_alpha, grad_flags, as_stream(stream));
 }
 
 }  // extern "C"

@@ -84,7 +84,7 @@ int launch_project_backward(int64_t n, const float *mean, const float *qvec,
                             const gsx_camera &cam, const int32_t *counts,
                             const float *g_mean2d, const float *g_cov2d,
                             const float *g_alpha, float *g_mean, float *g_qvec,
-                            float *g_logs, float *g_alpha_logit, cudaStream_t s);
+                            float *g_logs, float *g_alpha_logit, int32_t flags, cudaStream_t s);
 
 int launch_project_forward_batch(const gsx_batch_view *views, int32_t n_views, int64_t max_n,
                                  float frustum_radius, float tile_radius, float *mean2d,
@@ -92,7 +92,8 @@ int launch_project_forward_batch(const gsx_batch_view *views, int32_t n_views, i
                                  int32_t *counts, cudaStream_t s);
 int launch_project_backward_batch(const gsx_batch_view *views, int32_t n_views, int64_t n,
                                   const int32_t *counts, const float *g_mean2d,
-                                  const float *g_cov2d, const float *g_alpha, cudaStream_t s);
+                                  const float *g_cov2d, const float *g_alpha, int32_t flags,
+                                  cudaStream_t s);
 
 struct RasterArgs {
   int64_t n, n_keys;  // Gaussians and list entries: bounds for start/end/ids

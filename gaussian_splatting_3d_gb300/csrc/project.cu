@@ -232,17 +232,50 @@ __global__ void __launch_bounds__(256)
 // Parity-mode backward of the projection (depth detached, J constant):
 // the part that depends on the view.  Adds dL/dmean (through
 // mean2d = p_xy / p_z) into gm and dL/dSigma = A^T Gc A into GS.
+// Rotation, scales and M = R diag(s) of one Gaussian (as project_one makes
+// them), shared by the view-dependent and the parameter parts of the backward.
+struct Frame {
+  Rot rot;
+  float s[3];
+  float M[3][3];
+};
+
+__device__ __forceinline__ void make_frame(float4 q, const float *__restrict__ log_scale,
+                                           int64_t g, Frame &f) {
+  quat_rot(q, f.rot);
+  f.s[0] = gsx_expf(log_scale[3 * g]);
+  f.s[1] = gsx_expf(log_scale[3 * g + 1]);
+  f.s[2] = gsx_expf(log_scale[3 * g + 2]);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) f.M[i][j] = f.s[j] * f.rot.R[i][j];
+}
+
+__device__ __forceinline__ void world_cov(const Frame &f, float (&S)[3][3]) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      S[i][k] = fmaf(f.M[i][2], f.M[k][2], fmaf(f.M[i][1], f.M[k][1], f.M[i][0] * f.M[k][0]));
+}
+
+// The view-dependent part of the backward for one (Gaussian, view):
+// dL/dmean2d and dL/dcov2d -> dL/dmean (added into gm) and dL/dSigma (added
+// into GS).  flags = 0 is the reference's gradient: mean2d = p_xy / stopgrad(z)
+// and J constant (gs/renderer.py:365-377, 408-417).  GSX_GRAD_DEPTH adds the
+// z term of mean2d, GSX_GRAD_JACOBIAN the dependence of J on p (Sig = the
+// world covariance, needed only then).
 __device__ __forceinline__ void accum_view_grad(const ProjCam &cam, float m0, float m1, float m2,
-                                                float2 gm2, float4 gc, float (&gm)[3],
+                                                float2 gm2, float4 gc, int32_t flags,
+                                                const float (&Sig)[3][3], float (&gm)[3],
                                                 float (&GS)[3][3]) {
   float v0 = m0 - cam.t[0], v1 = m1 - cam.t[1], v2 = m2 - cam.t[2];
   float p[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i)
     p[i] = fmaf(cam.W[i][2], v2, fmaf(cam.W[i][1], v1, cam.W[i][0] * v0));
-  const float gp0 = gm2.x / p[2], gp1 = gm2.y / p[2];
-#pragma unroll
-  for (int j = 0; j < 3; ++j) gm[j] += fmaf(cam.W[1][j], gp1, cam.W[0][j] * gp0);
+  float gp0 = gm2.x / p[2], gp1 = gm2.y / p[2], gp2 = 0.0f;
   float iz = 1.0f / p[2];
   float j02 = (-p[0] / p[2]) / p[2];
   float j12 = (-p[1] / p[2]) / p[2];
@@ -262,26 +295,53 @@ __device__ __forceinline__ void accum_view_grad(const ProjCam &cam, float m0, fl
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int k = 0; k < 3; ++k) GS[i][k] += fmaf(A[1][i], B[1][k], A[0][i] * B[0][k]);
+  if (flags & (GSX_GRAD_DEPTH | GSX_GRAD_JACOBIAN)) {
+    const float iz2 = iz * iz;
+    if (flags & GSX_GRAD_DEPTH) gp2 = -fmaf(gm2.x, p[0], gm2.y * p[1]) * iz2;
+    if (flags & GSX_GRAD_JACOBIAN) {
+      // cov2d = A Sig A^T, A = J(p) W: dL/dA = (Gc + Gc^T) A Sig, dL/dJ = dL/dA W^T,
+      // with J00 = J11 = 1/z, J02 = -x/z^2, J12 = -y/z^2
+      float AS[2][3];
+#pragma unroll
+      for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+          AS[a][k] = fmaf(A[a][2], Sig[2][k], fmaf(A[a][1], Sig[1][k], A[a][0] * Sig[0][k]));
+      const float h00 = 2.0f * gc.x, h01 = gc.y + gc.z, h11 = 2.0f * gc.w;
+      float gA[2][3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        gA[0][k] = fmaf(h01, AS[1][k], h00 * AS[0][k]);
+        gA[1][k] = fmaf(h11, AS[1][k], h01 * AS[0][k]);
+      }
+      float gJ[2][3];
+#pragma unroll
+      for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          gJ[a][j] = fmaf(gA[a][2], cam.W[j][2], fmaf(gA[a][1], cam.W[j][1], gA[a][0] * cam.W[j][0]));
+      gp0 = fmaf(-gJ[0][2], iz2, gp0);
+      gp1 = fmaf(-gJ[1][2], iz2, gp1);
+      const float t2 = 2.0f * fmaf(gJ[0][2], p[0], gJ[1][2] * p[1]) * (iz2 * iz);
+      gp2 = fmaf(-(gJ[0][0] + gJ[1][1]), iz2, gp2 + t2);
+    }
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      gm[j] += fmaf(cam.W[2][j], gp2, fmaf(cam.W[1][j], gp1, cam.W[0][j] * gp0));
+  } else {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) gm[j] += fmaf(cam.W[1][j], gp1, cam.W[0][j] * gp0);
+  }
 }
 
 // The view-independent part: dL/dSigma -> quaternion and log-scale, and the
-// opacity logit.
-__device__ __forceinline__ void finish_param_grad(float4 q, const float *__restrict__ log_scale,
-                                                  float alpha_logit, int64_t g,
-                                                  const float (&GS)[3][3], float g_alpha,
+// opacity logit (zero where min(alpha, 0.99) clamps, with GSX_GRAD_CLAMP).
+__device__ __forceinline__ void finish_param_grad(const Frame &f, float4 q, float alpha_logit,
+                                                  int64_t g, const float (&GS)[3][3],
+                                                  float g_alpha, int32_t flags,
                                                   float *__restrict__ g_logs, float4 &g_q,
                                                   float &g_al) {
-  Rot rot;
-  quat_rot(q, rot);
-  float s[3];
-  s[0] = gsx_expf(log_scale[3 * g]);
-  s[1] = gsx_expf(log_scale[3 * g + 1]);
-  s[2] = gsx_expf(log_scale[3 * g + 2]);
-  float M[3][3];
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) M[i][j] = s[j] * rot.R[i][j];
+  const Rot &rot = f.rot;
   float GR[3][3];
   float gsc[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
@@ -290,12 +350,12 @@ __device__ __forceinline__ void finish_param_grad(float4 q, const float *__restr
     for (int j = 0; j < 3; ++j) {
       float acc = 0.0f;
 #pragma unroll
-      for (int k = 0; k < 3; ++k) acc = fmaf(GS[i][k] + GS[k][i], M[k][j], acc);
-      GR[i][j] = acc * s[j];
+      for (int k = 0; k < 3; ++k) acc = fmaf(GS[i][k] + GS[k][i], f.M[k][j], acc);
+      GR[i][j] = acc * f.s[j];
       gsc[j] = fmaf(acc, rot.R[i][j], gsc[j]);
     }
 #pragma unroll
-  for (int j = 0; j < 3; ++j) g_logs[3 * g + j] = gsc[j] * s[j];
+  for (int j = 0; j < 3; ++j) g_logs[3 * g + j] = gsc[j] * f.s[j];
   const float w = rot.w, x = rot.x, y = rot.y, z = rot.z;
   float gw = 2.0f * (-z * GR[0][1] + y * GR[0][2] + z * GR[1][0] - x * GR[1][2] -
                      y * GR[2][0] + x * GR[2][1]);
@@ -314,7 +374,7 @@ __device__ __forceinline__ void finish_param_grad(float4 q, const float *__restr
     g_q = make_float4(gw / 1e-12f, gx / 1e-12f, gy / 1e-12f, gz / 1e-12f);
   }
   float a = gsx_sigmoidf(alpha_logit);
-  g_al = g_alpha * (a * (1.0f - a));
+  g_al = ((flags & GSX_GRAD_CLAMP) && a > 0.99f) ? 0.0f : g_alpha * (a * (1.0f - a));
 }
 
 __global__ void __launch_bounds__(256)
@@ -328,7 +388,7 @@ __global__ void __launch_bounds__(256)
                             const float *__restrict__ g_alpha,
                             float *__restrict__ g_mean, float4 *__restrict__ g_qvec,
                             float *__restrict__ g_logs,
-                            float *__restrict__ g_alpha_logit) {
+                            float *__restrict__ g_alpha_logit, int32_t flags) {
   int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n) return;
   if (counts[g] == 0) {
@@ -342,13 +402,18 @@ __global__ void __launch_bounds__(256)
     g_alpha_logit[g] = 0.0f;
     return;
   }
+  const float4 q = qvec[g];
+  Frame f;
+  make_frame(q, log_scale, g, f);
+  float Sig[3][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};
+  if (flags & GSX_GRAD_JACOBIAN) world_cov(f, Sig);
   float gm[3] = {0.0f, 0.0f, 0.0f};
   float GS[3][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};
-  accum_view_grad(cam, mean[3 * g], mean[3 * g + 1], mean[3 * g + 2], g_mean2d[g], g_cov2d[g], gm,
-                  GS);
+  accum_view_grad(cam, mean[3 * g], mean[3 * g + 1], mean[3 * g + 2], g_mean2d[g], g_cov2d[g],
+                  flags, Sig, gm, GS);
 #pragma unroll
   for (int j = 0; j < 3; ++j) g_mean[3 * g + j] = gm[j];
-  finish_param_grad(qvec[g], log_scale, alpha_logit[g], g, GS, g_alpha[g], g_logs, g_qvec[g],
+  finish_param_grad(f, q, alpha_logit[g], g, GS, g_alpha[g], flags, g_logs, g_qvec[g],
                     g_alpha_logit[g]);
 }
 
@@ -360,7 +425,7 @@ __global__ void __launch_bounds__(256)
                                   const int32_t *__restrict__ counts,
                                   const float2 *__restrict__ g_mean2d,
                                   const float4 *__restrict__ g_cov2d,
-                                  const float *__restrict__ g_alpha) {
+                                  const float *__restrict__ g_alpha, int32_t flags) {
   const gsx_batch_view &v0 = views[0];
   const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= v0.n_gaussians) return;
@@ -368,12 +433,18 @@ __global__ void __launch_bounds__(256)
   float gm[3] = {0.0f, 0.0f, 0.0f};
   float GS[3][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};
   float ga = 0.0f;
+  const float4 q = reinterpret_cast<const float4 *>(v0.qvec)[g];
+  Frame f;
+  make_frame(q, v0.log_scale, g, f);
+  float Sig[3][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};
+  if (flags & GSX_GRAD_JACOBIAN) world_cov(f, Sig);
   bool seen = false;
   for (int vi = 0; vi < n_views; ++vi) {
     const int64_t item = views[vi].item_offset + g;
     if (counts[item] == 0) continue;
     seen = true;
-    accum_view_grad(proj_cam_of(views[vi].cam), m0, m1, m2, g_mean2d[item], g_cov2d[item], gm, GS);
+    accum_view_grad(proj_cam_of(views[vi].cam), m0, m1, m2, g_mean2d[item], g_cov2d[item], flags,
+                    Sig, gm, GS);
     ga += g_alpha[item];
   }
   float4 *g_qvec = reinterpret_cast<float4 *>(v0.g_qvec);
@@ -391,8 +462,7 @@ __global__ void __launch_bounds__(256)
   for (int j = 0; j < 3; ++j) v0.g_mean[3 * g + j] = gm[j];
   float4 gq;
   float gal;
-  finish_param_grad(reinterpret_cast<const float4 *>(v0.qvec)[g], v0.log_scale,
-                    v0.alpha_logit[g], g, GS, ga, v0.g_log_scale, gq, gal);
+  finish_param_grad(f, q, v0.alpha_logit[g], g, GS, ga, flags, v0.g_log_scale, gq, gal);
   g_qvec[g] = gq;
   v0.g_alpha_logit[g] = gal;
 }
@@ -417,12 +487,13 @@ int launch_project_forward_batch(const gsx_batch_view *views, int32_t n_views, i
 
 int launch_project_backward_batch(const gsx_batch_view *views, int32_t n_views, int64_t n,
                                   const int32_t *counts, const float *g_mean2d,
-                                  const float *g_cov2d, const float *g_alpha, cudaStream_t s) {
+                                  const float *g_cov2d, const float *g_alpha, int32_t flags,
+                                  cudaStream_t s) {
   if (n == 0 || n_views == 0) return GSX_OK;
   count_launches(1);
   project_backward_batch_kernel<<<grid_for(n, 256), 256, 0, s>>>(
       views, n_views, counts, reinterpret_cast<const float2 *>(g_mean2d),
-      reinterpret_cast<const float4 *>(g_cov2d), g_alpha);
+      reinterpret_cast<const float4 *>(g_cov2d), g_alpha, flags);
   return cuda_status(cudaGetLastError(), "project_backward_batch_kernel launch");
 }
 
@@ -459,14 +530,15 @@ int launch_project_backward(int64_t n, const float *mean, const float *qvec,
                             const gsx_camera &cam, const int32_t *counts,
                             const float *g_mean2d, const float *g_cov2d,
                             const float *g_alpha, float *g_mean, float *g_qvec,
-                            float *g_logs, float *g_alpha_logit, cudaStream_t s) {
+                            float *g_logs, float *g_alpha_logit, int32_t flags,
+                            cudaStream_t s) {
   if (n == 0) return GSX_OK;
   count_launches(1);
   project_backward_kernel<<<grid_for(n, 256), 256, 0, s>>>(
       n, mean, reinterpret_cast<const float4 *>(qvec), log_scale, alpha_logit,
       make_proj_cam(cam), counts, reinterpret_cast<const float2 *>(g_mean2d),
       reinterpret_cast<const float4 *>(g_cov2d), g_alpha, g_mean,
-      reinterpret_cast<float4 *>(g_qvec), g_logs, g_alpha_logit);
+      reinterpret_cast<float4 *>(g_qvec), g_logs, g_alpha_logit, flags);
   return cuda_status(cudaGetLastError(), "project_backward_kernel launch");
 }
 

@@ -69,6 +69,20 @@ class RasterSettings:
     tile_culling_radius: float = 6.0
     T_thresh: float = 0.01
     sh_order: int | None = None  # C used for colour (now_C); None = all coefficients
+    # gradient semantics: the reference detaches depth in mean2d (depth_detach,
+    # gs/sh_renderer.py:144), builds J without gradient and ignores the opacity
+    # clamp; exact_grad=True gives the true derivative of the image
+    depth_detach: bool = True
+    exact_grad: bool = False
+    # memory mode: hold only the tile lists between forward and backward (the
+    # projection is re-run in backward, bit-identically; the binning workspace
+    # is released after each forward)
+    recompute_projection: bool = False
+
+    def grad_flags(self) -> int:
+        if self.exact_grad:
+            return _lib.GSX_GRAD_EXACT
+        return 0 if self.depth_detach else _lib.GSX_GRAD_DEPTH
 
     def tiles(self, cam: CameraInfo):
         return (cam.w + self.tile_w - 1) // self.tile_w, (cam.h + self.tile_h - 1) // self.tile_h
@@ -93,6 +107,12 @@ class BinningBuffers:
             self.capacity = cap
             self.n = n
         return self
+
+    def release(self):
+        self.ws = None
+        self.ids = None
+        self.capacity = 0
+        self.n = -1
 
 
 _buffers: dict = {}
@@ -244,14 +264,20 @@ class ViewPipeline:
         # keep the capacity near 1.25 K so the sort grids stay small
         if K * 2 < self.key_capacity:
             self.key_capacity = max(int(K * 1.25) + 4096, 1 << 16)
+        if settings.recompute_projection:
+            pr = None
+            _bin_buffers(dev).release()
         return dict(pr=pr, ids=ids, start=start, end=end, K=K, cap=cap, topleft=topleft, c2w_dev=c2w_dev,
-                    out=out, params=params, gcam=gcam)
+                    out=out, params=params, gcam=gcam, grad_flags=settings.grad_flags(), settings=settings)
 
     def backward(self, state, mean, qvec, log_scale, sh, alpha_logit, grad_out, timer=None):
         dev = mean.device
         n = mean.shape[0]
         pr = state["pr"]
         ev = timer.stage if timer is not None else (lambda name: _null_ctx())
+        if pr is None:  # memory mode: the same projection again (deterministic, bit-identical)
+            with ev("project_recompute"):
+                pr = project(mean, qvec, log_scale, alpha_logit, state["gcam"], state["settings"])
         grad_out = grad_out.contiguous()
         g_mean2d = torch.zeros((n, 2), dtype=torch.float32, device=dev)
         g_cov2d = torch.zeros((n, 4), dtype=torch.float32, device=dev)
@@ -269,7 +295,7 @@ class ViewPipeline:
         with ev("project_bwd"):
             _lib.call("gsx_project_backward", n, ptr(mean), ptr(qvec), ptr(log_scale), ptr(alpha_logit),
                       ctypes.byref(state["gcam"]), ptr(pr.counts), ptr(g_mean2d), ptr(g_cov2d), ptr(g_alpha),
-                      ptr(g_mean), ptr(g_q), ptr(g_ls), ptr(g_al), stream_handle(dev))
+                      ptr(g_mean), ptr(g_q), ptr(g_ls), ptr(g_al), state["grad_flags"], stream_handle(dev))
         return g_mean, g_q, g_ls, g_sh, g_al
 
 

@@ -162,3 +162,21 @@ def custom_workload(n: int, width: int, height: int, sh_degree: int, seed: int =
     view = View(look_at_c2w(radius * d), cam, tile)
     W = uniform(seed, 7, height * width * 3).reshape(height, width, 3).astype(np.float32)
     return Workload(f"custom_{n}_{width}x{height}_C{sh_degree + 1}", scene, [view], W)
+
+
+def diff_workload(seed: int = 0, n: int = 2000, width: int = 64, height: int = 64, sh_degree: int = 1,
+                  log_scale_mu: float = -3.0, alpha_mu: float = 0.0) -> Workload:
+    """Differentiation workload: Gaussians drawn as in ``small`` (means
+    U[-1,1]^3, log-scales N(log_scale_mu, 0.5), opacity logits
+    N(alpha_mu, 1), DC from RGB U[0,1]) with SH degree 1 (band 1 N(0, 0.3));
+    camera at (0,0,-4) looking at the origin, 60 deg, 64x64, 16x16 tiles;
+    loss weights W uniform in [0,1]."""
+    scene = make_scene(n, seed, mean_dist="uniform", log_scale_mu=log_scale_mu, log_scale_sigma=0.5,
+                       alpha_sigma=1.0, sh_degree=sh_degree, dc_from_rgb=True, rest_sigma=0.3)
+    if alpha_mu:
+        scene.alpha_logit = (scene.alpha_logit + np.float32(alpha_mu)).astype(np.float32)
+    cam = CameraInfo.from_vertical_fov(60.0, width, height)
+    view = View(look_at_c2w((0.0, 0.0, -4.0)), cam, 16)
+    W = uniform(seed, 7, height * width * 3).reshape(height, width, 3).astype(np.float32)
+    return Workload(f"diff_{n}_{width}x{height}_C{sh_degree + 1}", scene, [view], W)
+

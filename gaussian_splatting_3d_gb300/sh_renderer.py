@@ -34,7 +34,9 @@ class SHRenderer(torch.nn.Module):
             tile_w=int(get("tile_size", 16)), tile_h=int(get("tile_size", 16)),
             frustum_culling_radius=float(get("frustum_culling_radius", 1.0)),
             tile_culling_radius=float(get("tile_culling_radius", 6.0)),
-            T_thresh=float(get("T_thresh", 0.01)))
+            T_thresh=float(get("T_thresh", 0.01)),
+            depth_detach=bool(get("depth_detach", True)),
+            exact_grad=bool(get("exact_grad", False)))
         if pts is not None and rgb is not None:
             self.initialize(pts, rgb, float(get("svec_init", 0.02)), float(get("alpha_init", 0.5)))
 

@@ -42,6 +42,8 @@ const char *gsx_status_string(int status);
 /* Detail message of the last failing call on this host thread ("" if none). */
 const char *gsx_last_error(void);
 /* ABI version of this library (increments on any signature change). */
+/* 2: gsx_project_backward / gsx_batch_project_backward take grad_flags */
+#define GSX_ABI_VERSION 2
 int gsx_abi_version(void);
 /* Number of kernels this library has launched in this process so far. */
 uint64_t gsx_kernel_launch_count(void);
@@ -188,8 +190,9 @@ size_t gsx_batch_view_size(void);
  * All views share the tile shape and the SH order.  The binning is
  * asynchronous (read its key count with gsx_binning_status using I as the
  * Gaussian count).  gsx_batch_project_backward needs all views to share one
- * scene and writes that scene's gradients (views[0].g_*), summed over views;
- * the raster backward adds SH gradients into each view's g_sh.
+ * scene and writes that scene's gradients (views[0].g_*), summed over views
+ * (grad_flags as for gsx_project_backward); the raster backward adds SH
+ * gradients into each view's g_sh.
  */
 int gsx_batch_project_forward(const gsx_batch_view *views_dev, const gsx_batch_view *views_host,
                               int32_t n_views, float frustum_radius, float tile_radius,
@@ -212,7 +215,8 @@ int gsx_batch_render_backward(const gsx_batch_view *views_dev, const gsx_batch_v
                               float *g_cov2d, float *g_alpha, float T_thresh, void *stream);
 int gsx_batch_project_backward(const gsx_batch_view *views_dev, const gsx_batch_view *views_host,
                                int32_t n_views, const int32_t *counts, const float *g_mean2d,
-                               const float *g_cov2d, const float *g_alpha, void *stream);
+                               const float *g_cov2d, const float *g_alpha, int32_t grad_flags,
+                               void *stream);
 
 /*
  * One pass over n Gaussians (mean f32[n,3], qvec f32[n,4] WXYZ,
@@ -312,20 +316,29 @@ int gsx_render_backward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
                         void *stream);
 
 /*
- * Projection backward (parity mode: depth detached in mean2d = p_xy / p_z and
- * J constant, as gs/renderer.py:365-419 does) from the raster gradients
- * grad_mean2d f32[n,2], grad_cov2d f32[n,4], grad_alpha f32[n] to the
- * parameter gradients grad_mean f32[n,3], grad_qvec f32[n,4],
- * grad_log_scale f32[n,3], grad_alpha_logit f32[n] (overwritten; zero for
- * culled Gaussians, i.e. counts[i] == 0).
+ * Projection backward from the raster gradients grad_mean2d f32[n,2],
+ * grad_cov2d f32[n,4], grad_alpha f32[n] to the parameter gradients
+ * grad_mean f32[n,3], grad_qvec f32[n,4], grad_log_scale f32[n,3],
+ * grad_alpha_logit f32[n] (overwritten; zero for culled Gaussians, i.e.
+ * counts[i] == 0).  grad_flags = 0 gives the reference's gradient
+ * (gs/renderer.py:365-419: depth detached in mean2d = p_xy / p_z, J built
+ * without gradient; vol_render_sh.h:346: the opacity clamp min(alpha, 0.99)
+ * ignored).  GSX_GRAD_DEPTH adds the z term of mean2d (the reference's
+ * depth_detach=False), GSX_GRAD_JACOBIAN the gradient through J,
+ * GSX_GRAD_CLAMP zeroes the opacity gradient where the clamp is active;
+ * GSX_GRAD_EXACT (all three) is the true derivative of the rendered image.
  */
+#define GSX_GRAD_DEPTH 1
+#define GSX_GRAD_JACOBIAN 2
+#define GSX_GRAD_CLAMP 4
+#define GSX_GRAD_EXACT 7
 int gsx_project_backward(int64_t n, const float *mean, const float *qvec,
                          const float *log_scale, const float *alpha_logit,
                          const gsx_camera *cam, const int32_t *counts,
                          const float *grad_mean2d, const float *grad_cov2d,
                          const float *grad_alpha, float *grad_mean,
                          float *grad_qvec, float *grad_log_scale,
-                         float *grad_alpha_logit, void *stream);
+                         float *grad_alpha_logit, int32_t grad_flags, void *stream);
 
 #ifdef __cplusplus
 }

@@ -498,18 +498,27 @@ void orc_render_bwd(const orc_raster_params *P, const float *mean, const float *
 }
 
 /* ------------------------------------------------------------------------ */
-/* projection backward, parity mode: the autograd of gs/renderer.py:390-419  */
-/* with depth detached (mean2d = p_xy / stopgrad(p_z)) and J constant        */
-/* (@torch.no_grad jacobian), through kornia's normalised-quaternion         */
-/* rotation, svec = exp(.) and alpha = sigmoid(.) (utils/activations.py).    */
-/* Evaluated in double.                                                      */
+/* projection backward: the autograd of gs/renderer.py:390-419 through      */
+/* kornia's normalised-quaternion rotation, svec = exp(.) and                 */
+/* alpha = sigmoid(.) (utils/activations.py).  Evaluated in double.           */
+/* flags = 0 is the reference's gradient: depth detached                      */
+/* (mean2d = p_xy / stopgrad(p_z), gs/renderer.py:408-417), J constant        */
+/* (@torch.no_grad jacobian, gs/renderer.py:365-377) and the opacity clamp    */
+/* min(alpha, 0.99) ignored (vol_render_sh.h:346).  ORC_GRAD_DEPTH adds the   */
+/* z term of mean2d (the reference's depth_detach=False), ORC_GRAD_JACOBIAN   */
+/* the dependence of J on the camera-space mean, ORC_GRAD_CLAMP a zero        */
+/* opacity gradient where the clamp is active: all three give the true        */
+/* derivative of the rendered image.                                          */
 /* ------------------------------------------------------------------------ */
+#define ORC_GRAD_DEPTH 1
+#define ORC_GRAD_JACOBIAN 2
+#define ORC_GRAD_CLAMP 4
 void orc_project_bwd(int64_t n, const float *mean, const float *qvec,
                      const float *log_s, const float *alpha_logit,
                      const orc_camera *cam, const uint8_t *mask,
                      const float *g_mean2d, const float *g_cov2d,
                      const float *g_alpha, float *g_mean, float *g_qvec,
-                     float *g_logs, float *g_alpha_logit) {
+                     float *g_logs, float *g_alpha_logit, int32_t flags) {
   const float *c = cam->c2w;
   double Wm[3][3];
   for (int i = 0; i < 3; ++i)
@@ -524,11 +533,11 @@ void orc_project_bwd(int64_t n, const float *mean, const float *qvec,
     double v[3] = {(double)m[0] - c[3], (double)m[1] - c[7], (double)m[2] - c[11]};
     double p[3];
     for (int i = 0; i < 3; ++i) p[i] = Wm[i][0] * v[0] + Wm[i][1] * v[1] + Wm[i][2] * v[2];
-    /* mean2d = p_xy / z (z detached): dL/dp_xy = g / z */
-    double gp[3] = {g_mean2d[2 * g] / p[2], g_mean2d[2 * g + 1] / p[2], 0.0};
-    for (int j = 0; j < 3; ++j)
-      g_mean[3 * g + j] = (float)(Wm[0][j] * gp[0] + Wm[1][j] * gp[1] + Wm[2][j] * gp[2]);
-    /* A = first two rows of J W (constant) */
+    /* mean2d = p_xy / z: dL/dp_xy = g / z (z detached unless ORC_GRAD_DEPTH) */
+    const double gm2[2] = {g_mean2d[2 * g], g_mean2d[2 * g + 1]};
+    double gp[3] = {gm2[0] / p[2], gm2[1] / p[2], 0.0};
+    if (flags & ORC_GRAD_DEPTH) gp[2] = -(gm2[0] * p[0] + gm2[1] * p[1]) / (p[2] * p[2]);
+    /* A = first two rows of J W */
     double iz = 1.0 / p[2], j02 = -p[0] / p[2] / p[2], j12 = -p[1] / p[2] / p[2];
     double A[2][3];
     for (int k = 0; k < 3; ++k) {
@@ -546,7 +555,6 @@ void orc_project_bwd(int64_t n, const float *mean, const float *qvec,
           for (int b = 0; b < 2; ++b) acc += A[a][i] * Gc[a][b] * A[b][k];
         GS[i][k] = acc;
       }
-    /* Sigma = M M^T, M = R diag(s): dL/dM = (GS + GS^T) M */
     const float *q = qvec + 4 * g;
     double qn2 = (double)q[0] * q[0] + (double)q[1] * q[1] + (double)q[2] * q[2] + (double)q[3] * q[3];
     double nq = sqrt(qn2);
@@ -560,6 +568,30 @@ void orc_project_bwd(int64_t n, const float *mean, const float *qvec,
     double M[3][3], GM[3][3];
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) M[i][j] = R[i][j] * s[j];
+    if (flags & ORC_GRAD_JACOBIAN) {
+      /* cov2d = A Sigma A^T with A = J(p) W: dL/dA = (Gc + Gc^T) A Sigma,
+         dL/dJ = dL/dA W^T; J00 = J11 = 1/z, J02 = -x/z^2, J12 = -y/z^2 */
+      double Sig[3][3], AS[2][3], gA[2][3], gJ[2][3];
+      for (int i = 0; i < 3; ++i)
+        for (int k = 0; k < 3; ++k)
+          Sig[i][k] = M[i][0] * M[k][0] + M[i][1] * M[k][1] + M[i][2] * M[k][2];
+      for (int a = 0; a < 2; ++a)
+        for (int k = 0; k < 3; ++k)
+          AS[a][k] = A[a][0] * Sig[0][k] + A[a][1] * Sig[1][k] + A[a][2] * Sig[2][k];
+      for (int a = 0; a < 2; ++a)
+        for (int k = 0; k < 3; ++k)
+          gA[a][k] = (Gc[a][0] + Gc[0][a]) * AS[0][k] + (Gc[a][1] + Gc[1][a]) * AS[1][k];
+      for (int a = 0; a < 2; ++a)
+        for (int j = 0; j < 3; ++j)
+          gJ[a][j] = gA[a][0] * Wm[j][0] + gA[a][1] * Wm[j][1] + gA[a][2] * Wm[j][2];
+      const double iz2 = iz * iz;
+      gp[0] += -gJ[0][2] * iz2;
+      gp[1] += -gJ[1][2] * iz2;
+      gp[2] += -(gJ[0][0] + gJ[1][1]) * iz2 + 2.0 * (gJ[0][2] * p[0] + gJ[1][2] * p[1]) * iz2 * iz;
+    }
+    for (int j = 0; j < 3; ++j)
+      g_mean[3 * g + j] = (float)(Wm[0][j] * gp[0] + Wm[1][j] * gp[1] + Wm[2][j] * gp[2]);
+    /* Sigma = M M^T, M = R diag(s): dL/dM = (GS + GS^T) M */
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) {
         double acc = 0.0;
@@ -588,7 +620,9 @@ void orc_project_bwd(int64_t n, const float *mean, const float *qvec,
       for (int k = 0; k < 4; ++k) g_qvec[4 * g + k] = (float)(gu[k] / 1e-12);
     }
     double sa = 1.0 / (1.0 + exp(-(double)alpha_logit[g]));
-    g_alpha_logit[g] = (float)(g_alpha[g] * sa * (1.0 - sa));
+    /* the renderer uses min(alpha, 0.99) with alpha the float sigmoid */
+    const int clamped = (flags & ORC_GRAD_CLAMP) && sigmoidf_(alpha_logit[g]) > 0.99f;
+    g_alpha_logit[g] = clamped ? 0.0f : (float)(g_alpha[g] * sa * (1.0 - sa));
   }
 }
 

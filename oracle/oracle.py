@@ -188,7 +188,13 @@ def render_bwd(P: OrcRasterParams, mean2d, cov2d, sh, alpha, start, end, ids, to
     return g
 
 
-def project_bwd(mean, qvec, log_s, alpha_logit, cam: OrcCamera, mask, g_mean2d, g_cov2d, g_alpha):
+GRAD_DEPTH, GRAD_JACOBIAN, GRAD_CLAMP = 1, 2, 4
+GRAD_EXACT = GRAD_DEPTH | GRAD_JACOBIAN | GRAD_CLAMP
+
+
+def project_bwd(mean, qvec, log_s, alpha_logit, cam: OrcCamera, mask, g_mean2d, g_cov2d, g_alpha, flags: int = 0):
+    """flags = 0: the reference's gradient (depth detached, J constant, opacity
+    clamp ignored); GRAD_* bits add the true-derivative terms."""
     mean, qvec, log_s, alpha_logit = f32(mean), f32(qvec), f32(log_s), f32(alpha_logit)
     n = mean.shape[0]
     out = dict(mean=np.zeros((n, 3), np.float32), qvec=np.zeros((n, 4), np.float32),
@@ -196,7 +202,7 @@ def project_bwd(mean, qvec, log_s, alpha_logit, cam: OrcCamera, mask, g_mean2d, 
     m = np.ascontiguousarray(mask, dtype=np.uint8)
     lib().orc_project_bwd(c_int64(n), _p(mean), _p(qvec), _p(log_s), _p(alpha_logit), ctypes.byref(cam), _p(m),
                           _p(f32(g_mean2d)), _p(f32(g_cov2d)), _p(f32(g_alpha)), _p(out["mean"]), _p(out["qvec"]),
-                          _p(out["log_scale"]), _p(out["alpha_logit"]))
+                          _p(out["log_scale"]), _p(out["alpha_logit"]), ctypes.c_int32(flags))
     return out
 
 
@@ -205,7 +211,7 @@ def num_threads() -> int:
 
 
 def render_view(scene, view, grad_weight=None, frustum_radius=1.0, tile_radius=6.0, T_thresh=0.01,
-                sh_order=None):
+                sh_order=None, grad_flags: int = 0):
     """Full oracle pipeline for one view of a scene.Scene / scene.View:
     project, bin, raster forward and (if grad_weight is given) backward
     through the projection.  Returns a dict of every intermediate."""
@@ -230,7 +236,7 @@ def render_view(scene, view, grad_weight=None, frustum_radius=1.0, tile_radius=6
         g = render_bwd(P, pr["mean2d"], pr["cov2d"], scene.sh, pr["alpha"], b["start"], b["end"], b["ids"],
                        topleft, view.c2w, psx, psy, img, grad_weight)
         gp = project_bwd(scene.mean, scene.qvec, scene.log_scale, scene.alpha_logit, ocam, pr["mask"],
-                         g["mean2d"], g["cov2d"], g["alpha"])
+                         g["mean2d"], g["cov2d"], g["alpha"], grad_flags)
         res["raster_grads"] = g
         res["param_grads"] = dict(gp, sh=g["sh"])
     return res

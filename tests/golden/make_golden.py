@@ -2,7 +2,7 @@
 
 Run here (the only machine with the reference sources):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [fixture names...]
 
 What runs is the reference's own code:
   * its Python, imported unmodified from /root/reference: ``SHRenderer.forward``
@@ -262,6 +262,11 @@ def cases():
     ties = S.Scene(np.repeat(sc.mean * 0, n, 0), np.repeat(sc.qvec, n, 0), np.full((n, 3), -2.5, np.float32),
                    np.repeat(sc.sh, n, 0), np.linspace(-2, 2, n).astype(np.float32), 2)
     out.append(("ties_60_64x48", S.Workload("ties", ties, base.views, base.grad_weight), None))
+    # the differentiation workload (2,000 Gaussians, 64x64, SH degree 1), and a
+    # variant with larger, more opaque Gaussians where the 0.99 opacity clamp
+    # and the transmittance cut-off are active
+    out.append(("diff_2k_64_C2", S.diff_workload(), None))
+    out.append(("diff_clamp_2k_64_C2", S.diff_workload(log_scale_mu=-2.0, alpha_mu=3.0), None))
     return out
 
 
@@ -274,7 +279,10 @@ def main():
     sys.modules["_gs"] = gs_mod
     sys.path.insert(0, str(REF))
     torch.set_num_threads(8)
+    only = set(sys.argv[1:])  # optional: names of the fixtures to (re)generate
     for name, wl, now_C in cases():
+        if only and name not in only:
+            continue
         view = wl.views[0]
         cam = view.cam
         fix = run_case(gs_mod, name, wl.scene, view.c2w, (cam.fx, cam.fy, cam.cx, cam.cy, cam.w, cam.h),
