@@ -572,12 +572,23 @@ def run_memory(args):
     print(json.dumps(line), flush=True)
 
 
+def run_reference_cuda(args):
+    """The reference's own CUDA extension on this GPU is not run: built from
+    its sources for sm_103a, its SH raster backward stopped at its device-side
+    assert that the recomputed colour equals the forward's bit for bit
+    (gs/src/include/vol_render_sh.h:448-452) on the 1M-Gaussian 1920x1080
+    workload, and the GPU logged Xid 43.  Reference GPU code that faulted is
+    not run again."""
+    print(json.dumps({"impl": "reference-cuda", "unavailable":
+                      "the reference's CUDA backward trips its own device assert (vol_render_sh.h:448-452: "
+                      "recomputed colour != stored colour) on GB300; faulting reference GPU code is not re-run"}))
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--impl", default="gsx", choices=["gsx", "reference"])
+    ap.add_argument("--impl", default="gsx", choices=["gsx", "reference", "reference-cuda"])
     ap.add_argument("--workload", default="headline", choices=["headline", "small", "batch", "serve", "memory"])
     ap.add_argument("--views", type=int, default=32)
     ap.add_argument("--n-batch", type=int, default=500_000)
@@ -597,6 +608,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.impl == "reference-cuda":
+        run_reference_cuda(args)
     elif args.workload == "batch":
         run_batch(args)
     elif args.workload == "serve":

@@ -39,66 +39,7 @@ REF = Path("/root/reference")
 sys.path.insert(0, str(ROOT))
 
 from oracle import build_ref  # noqa: E402
-
-
-# --------------------------------------------------------------------------
-# stand-ins for modules the reference imports but this container lacks
-# --------------------------------------------------------------------------
-def _install_stubs():
-    def mod(name, **attrs):
-        m = types.ModuleType(name)
-        m.__dict__.update(attrs)
-        sys.modules[name] = m
-        return m
-
-    mod("cv2")
-    mpl = mod("matplotlib")
-    mpl.pyplot = mod("matplotlib.pyplot")
-    mod("faiss")
-
-    class _TT:
-        def __class_getitem__(cls, item):
-            return torch.Tensor
-
-    mod("torchtyping", TensorType=_TT)
-
-    class QuaternionCoeffOrder:
-        XYZW = "xyzw"
-        WXYZ = "wxyz"
-
-    def quaternion_to_rotation_matrix(quaternion, order=QuaternionCoeffOrder.WXYZ):
-        q = torch.nn.functional.normalize(quaternion, p=2.0, dim=-1, eps=1e-12)
-        if order == QuaternionCoeffOrder.XYZW:
-            x, y, z, w = torch.chunk(q, chunks=4, dim=-1)
-        else:
-            w, x, y, z = torch.chunk(q, chunks=4, dim=-1)
-        tx, ty, tz = 2.0 * x, 2.0 * y, 2.0 * z
-        twx, twy, twz = tx * w, ty * w, tz * w
-        txx, txy, txz = tx * x, ty * x, tz * x
-        tyy, tyz, tzz = ty * y, tz * y, tz * z
-        one = torch.tensor(1.0)
-        m = torch.stack([one - (tyy + tzz), txy - twz, txz + twy,
-                         txy + twz, one - (txx + tzz), tyz - twx,
-                         txz - twy, tyz + twx, one - (txx + tyy)], dim=-1)
-        return m.view(quaternion.shape[:-1] + (3, 3))
-
-    def rotation_matrix_to_quaternion(*a, **k):  # imported, never called on this path
-        raise NotImplementedError
-
-    conv = mod("kornia.geometry.conversions", QuaternionCoeffOrder=QuaternionCoeffOrder,
-               quaternion_to_rotation_matrix=quaternion_to_rotation_matrix,
-               rotation_matrix_to_quaternion=rotation_matrix_to_quaternion)
-    geo = mod("kornia.geometry", conversions=conv)
-    mod("kornia", geometry=geo)
-
-    class _Cudart:
-        def cudaProfilerStart(self):
-            return 0
-
-        def cudaProfilerStop(self):
-            return 0
-
-    torch.cuda.profiler.cudart = lambda: _Cudart()
+from oracle.ref_stubs import install_stubs, reference_cfg  # noqa: E402
 
 
 # --------------------------------------------------------------------------
@@ -162,21 +103,6 @@ class EmulatedGs(types.ModuleType):
                                 ctypes.c_float(pixel_size_y), u(H), u(W), ctypes.c_float(thresh))
         self.log["bwd"] = dict(grad_mean=grad_mean.clone(), grad_cov=grad_cov.clone(),
                                grad_sh=grad_sh_coeffs.clone(), grad_alpha=grad_alpha.clone())
-
-
-class Cfg(dict):
-    __getattr__ = dict.__getitem__
-
-
-def reference_cfg(C_max: int, tile: int) -> Cfg:
-    # renderer keys as in conf/garden_sh.yaml:19-46; training keys are unused here
-    return Cfg(device="cpu", sh_order=C_max, svec_act="exp", alpha_act="sigmoid", tile_size=tile,
-               near_plane=1.5, far_plane=1000.0, frustum_culling_radius=1.0, tile_culling_type="aabb",
-               tile_culling_thresh=0.01, tile_culling_radius=6.0, T_thresh=0.01, sh_upgrades=[2000, 4000],
-               adaptive_control_iteration=800, pos_grad_thresh=0.0002, split_scale_thresh=0.02,
-               scale_shrink_factor=1.6, alpha_reset_period=100000000, remove_low_alpha_period=10000000,
-               alpha_reset_val=0.1, alpha_thresh=0.05, max_iteration=10000, mean_lr=1e-3, qvec_lr=1e-2,
-               svec_lr=1e-2, sh_coeffs_lr=1e-2, alpha_lr=1e-2, warmup_steps=0, debug=False)
 
 
 def canonical_ids(ids, keys):
@@ -274,7 +200,7 @@ def main():
     if not build_ref.reference_available():
         raise SystemExit("the reference sources are needed to generate fixtures")
     lib = build_ref.build()
-    _install_stubs()
+    install_stubs(cpu_only=True)
     gs_mod = EmulatedGs(lib)
     sys.modules["_gs"] = gs_mod
     sys.path.insert(0, str(REF))
