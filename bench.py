@@ -39,6 +39,23 @@ sys.path.insert(0, ROOT)
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 
 
+def profiled_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch of `kernel` (dram__bytes_read.sum +
+    dram__bytes_write.sum) from the committed ncu summary of `workload`, or
+    None when no capture covers it."""
+    import glob
+    import re
+
+    pat = re.compile(rf"^traffic_bytes_per_launch {re.escape(kernel)} {re.escape(workload)}: (\d+)\s*$")
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
+        with open(path) as f:
+            for line in f:
+                m = pat.match(line)
+                if m:
+                    return int(m.group(1)), os.path.relpath(path, ROOT)
+    return None
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -259,6 +276,12 @@ def run_gsx(args):
         "gpu_launches": launches,
         "wall_s": round(wall1 - wall0, 3),
     }
+    prof = profiled_traffic(dom, args.workload) if args.n == 1_000_000 else None
+    if prof is not None:
+        line["roofline"]["traffic"] = prof[0]
+        line["roofline"]["traffic_source"] = f"ncu dram__bytes_read.sum + dram__bytes_write.sum, {prof[1]}"
+    line["roofline"]["note"] = ("raster kernels are FP32/SFU-issue bound (see profiles/); the HBM fraction "
+                                "counts each key's Gaussian record once per tile")
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(wl, args.cpu_frac)
     print(json.dumps(line), flush=True)
