@@ -250,11 +250,14 @@ struct SmemLayout {
   float2 *box;  // half-extents of the region where the pair may contribute
   float *alpha;
   int *ids;
+  float *inv_det;  // 1 / det(cov), backward only
   float *sh;
 };
 
-// Shared-memory layout of one batch of B Gaussians (B even): 10*B floats of
-// records followed by the SH rows, which start 16-byte aligned.
+constexpr int kRecordFloats = 12;  // floats of per-Gaussian records per batch slot
+
+// Shared-memory layout of one batch of B Gaussians (B a multiple of 4):
+// kRecordFloats*B floats of records followed by the SH rows (16-byte aligned).
 template <int C>
 __device__ __forceinline__ SmemLayout carve(float *smem, int B) {
   SmemLayout L;
@@ -263,7 +266,8 @@ __device__ __forceinline__ SmemLayout carve(float *smem, int B) {
   L.box = reinterpret_cast<float2 *>(smem + 6 * B);
   L.alpha = smem + 8 * B;
   L.ids = reinterpret_cast<int *>(smem + 9 * B);
-  L.sh = smem + 10 * B;
+  L.inv_det = smem + 10 * B;
+  L.sh = smem + kRecordFloats * B;
   return L;
 }
 
@@ -302,8 +306,9 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 
 // Gather one batch of the tile's list into shared memory, keeping only the
 // Gaussians whose skip box meets the tile's pixel centres (in list order).
-// Requires nb <= blockDim.x.  Returns the number kept.
-template <int C>
+// Requires nb <= blockDim.x.  Returns the number kept.  INV_DET also stores
+// 1 / det(cov) (the same operation the per-pair code would do).
+template <int C, bool INV_DET>
 __device__ __forceinline__ int load_batch(const RasterArgs &a, const ViewCtx &ctx,
                                           const SmemLayout &L, int first, int nb, int t, int nthr,
                                           float tx0, float tx1, float ty0, float ty1,
@@ -346,6 +351,7 @@ __device__ __forceinline__ int load_batch(const RasterArgs &a, const ViewCtx &ct
     L.cov[pos] = cv;
     L.alpha[pos] = al;
     L.box[pos] = box;
+    if constexpr (INV_DET) L.inv_det[pos] = 1.0f / fmaf(cv.x, cv.w, -(cv.y * cv.z));
   }
   __syncthreads();
   const int count = total * 3 * CC;
@@ -359,6 +365,41 @@ __device__ __forceinline__ int load_batch(const RasterArgs &a, const ViewCtx &ct
   }
   __syncthreads();
   return total;
+}
+
+// Bounds of the pixel centres of this warp's block (min/max over its lanes).
+__device__ __forceinline__ float4 warp_block(float px, float py) {
+  float x0 = px, x1 = px, y0 = py, y1 = py;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    x0 = fminf(x0, __shfl_xor_sync(kFull, x0, o));
+    x1 = fmaxf(x1, __shfl_xor_sync(kFull, x1, o));
+    y0 = fminf(y0, __shfl_xor_sync(kFull, y0, o));
+    y1 = fmaxf(y1, __shfl_xor_sync(kFull, y1, o));
+  }
+  return make_float4(x0, x1, y0, y1);
+}
+
+// This warp's list of the batch Gaussians (batch positions, in order) whose
+// skip box meets the warp's pixel block; the others are skipped by every
+// lane of the warp, so leaving them out changes nothing.  All lanes call it.
+__device__ __forceinline__ int warp_list(const SmemLayout &L, int nk, float4 blk, int *wl,
+                                         int lane) {
+  int cnt = 0;
+  for (int c = 0; c < nk; c += 32) {
+    const int i = c + lane;
+    bool hit = false;
+    if (i < nk) {
+      const float2 m = L.mean[i], h = L.box[i];
+      hit = !(m.x + h.x < blk.x) && !(m.x - h.x > blk.y) && !(m.y + h.y < blk.z) &&
+            !(m.y - h.y > blk.w);
+    }
+    const unsigned b = __ballot_sync(kFull, hit);
+    if (hit) wl[cnt + __popc(b & lanemask_lt())] = i;
+    cnt += __popc(b);
+  }
+  __syncwarp();
+  return cnt;
 }
 
 template <int C>
@@ -377,9 +418,10 @@ __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a
   const int nthr = blockDim.x;
   const int B = a.batch;
   SmemLayout L = carve<C>(reinterpret_cast<float *>(smem4), B);
+  int *wl = reinterpret_cast<int *>(L.sh + B * GSH) + (threadIdx.x >> 5) * B;  // [nwarps][B]
 
   const ViewCtx ctx = make_ctx<BATCHED>(a);
-  const int t = threadIdx.x;
+  const int t = threadIdx.x, lane = t & 31;
   int gx, gy;
   pixel_of(ctx, t, gx, gy);
   const bool inside = t < ctx.tile_w * ctx.tile_h && gx < ctx.width && gy < ctx.height;
@@ -407,14 +449,17 @@ __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a
   bool done = !inside;
   float tx0, tx1, ty0, ty1;
   tile_bounds(ctx, tx0, tx1, ty0, ty1);
+  const float4 blk = warp_block(px, py);
 
   for (int base = 0; base < n; base += B) {
     if (__syncthreads_and(done)) break;
     const int nb = min(B, n - base);
     const int nk =
-        load_batch<C>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1, s_wcount);
+        load_batch<C, false>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1, s_wcount);
+    const int nw = __all_sync(kFull, done) ? 0 : warp_list(L, nk, blk, wl, lane);
     if (!done) {
-      for (int i = 0; i < nk; ++i) {
+      for (int j = 0; j < nw; ++j) {
+        const int i = wl[j];
         if (T < thr) {
           done = true;
           break;
@@ -494,7 +539,19 @@ __device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], 
 
 constexpr int kSlots = 5;     // Gaussians per warp matrix product (15 of 16 rows)
 constexpr int kWStride = 36;  // row stride of the 16 x 32 weight matrix (bank-conflict free)
-constexpr int kYStride = 24;  // row stride of the 32 x 16 basis matrix (bank-conflict free)
+constexpr int kYStride = 36;  // row stride of the basis, stored k-major: 16 rows of 32 pixels
+                              // (conflict-free both for the per-pixel writes and the
+                              // B-fragment reads: bank = 4 g + tq + const)
+
+// Per-Gaussian gradient record in shared memory: 6 scalars, then 3 SH
+// channels with a channel stride that keeps the three channels' atomics of
+// one mma fragment on distinct banks (20 for C = 4: windows 0-7, 20-27, 8-15).
+template <int C>
+struct Grad {
+  static constexpr int CC = C * C;
+  static constexpr int CSTR = CC == 16 ? 20 : CC;
+  static constexpr int NV = 6 + 3 * CSTR;
+};
 
 // SH gradients of the staged Gaussians: D[r][k] = sum_p W[r][p] * Y[p][k] for
 // rows r = 3*slot + channel, added into the batch accumulators.
@@ -503,7 +560,7 @@ __device__ __forceinline__ void flush_sh_group(const float *Ws, const float *Ys,
                                                int nslot, float *s_grad, int lane) {
   constexpr int CC = Sh<C>::CC;
   constexpr int NT = (CC + 7) / 8;
-  constexpr int NV = 6 + 3 * CC;
+  constexpr int NV = Grad<C>::NV, CSTR = Grad<C>::CSTR;
   const int g = lane >> 2, tq = lane & 3;
   float d[NT][4];
 #pragma unroll
@@ -518,8 +575,8 @@ __device__ __forceinline__ void flush_sh_group(const float *Ws, const float *Ys,
 #pragma unroll
     for (int nt = 0; nt < NT; ++nt) {
       uint32_t b0h, b0l, b1h, b1l;
-      split_tf32(Ys[(8 * ks + tq) * kYStride + 8 * nt + g], b0h, b0l);
-      split_tf32(Ys[(8 * ks + tq + 4) * kYStride + 8 * nt + g], b1h, b1l);
+      split_tf32(Ys[(8 * nt + g) * kYStride + 8 * ks + tq], b0h, b0l);
+      split_tf32(Ys[(8 * nt + g) * kYStride + 8 * ks + tq + 4], b1h, b1l);
       mma_tf32(d[nt], ah, b0h, b1h);
       mma_tf32(d[nt], ah, b0l, b1l);
       mma_tf32(d[nt], al, b0h, b1h);
@@ -534,7 +591,7 @@ __device__ __forceinline__ void flush_sh_group(const float *Ws, const float *Ys,
       const int k = 8 * nt + 2 * tq + (e & 1);
       if (r < rows && k < CC && d[nt][e] != 0.0f) {
         const int slot = r / 3, ch = r - 3 * slot;
-        atomicAdd(&s_grad[slots[slot] * NV + 6 + ch * CC + k], d[nt][e]);
+        atomicAdd(&s_grad[slots[slot] * NV + 6 + ch * CSTR + k], d[nt][e]);
       }
     }
 }
@@ -543,7 +600,7 @@ template <int C, int MAXT, bool BATCHED>
 __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1)
     raster_backward_kernel(const RasterArgs a) {
   constexpr int CC = Sh<C>::CC, CCP = Sh<C>::CCP, GSH = Sh<C>::GSH;
-  constexpr int NV = 6 + 3 * CC;  // gm0 gm1 gc0 gc12 gc3 galpha gsh[3*CC]
+  constexpr int NV = Grad<C>::NV, CSTR = Grad<C>::CSTR;  // gm0 gm1 gc0 gc12 gc3 galpha gsh
   extern __shared__ float4 smem4[];
   __shared__ int s_wcount[32];
   float *smem = reinterpret_cast<float *>(smem4);
@@ -552,9 +609,10 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
   SmemLayout L = carve<C>(smem, B);
   float *s_grad = L.sh + B * GSH;                                         // [B][NV]
   float *s_w = s_grad + B * NV;                                           // [nwarps][16][kWStride]
-  float *s_y = s_w + nwarps * 16 * kWStride;                              // [nwarps][32][kYStride]
-  int *s_slots = reinterpret_cast<int *>(s_y + nwarps * 32 * kYStride);  // [nwarps][8]
+  float *s_y = s_w + nwarps * 16 * kWStride;                              // [nwarps][16][kYStride]
+  int *s_slots = reinterpret_cast<int *>(s_y + nwarps * 16 * kYStride);  // [nwarps][8]
   int *s_touched = s_slots + nwarps * 8;                                  // [B]
+  int *wl = s_touched + B + (threadIdx.x >> 5) * B;                       // [nwarps][B]
 
   const ViewCtx ctx = make_ctx<BATCHED>(a);
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -568,14 +626,14 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
   const float py = fmaf((float)gy, ctx.psy, ctx.topleft[1]);
   float2 Y2[Sh<C>::NY2];
   float *Ws = s_w + warp * 16 * kWStride;
-  float *Ys = s_y + warp * 32 * kYStride;
+  float *Ys = s_y + warp * 16 * kYStride;
   int *slots = s_slots + warp * 8;
   {
     float Y[CC];
     sh_basis<C>(ctx.c2w, px, py, Y);
     pack_basis<C>(Y, Y2);
 #pragma unroll
-    for (int k = 0; k < 16; ++k) Ys[lane * kYStride + k] = k < CC ? Y[k < CC ? k : 0] : 0.0f;
+    for (int k = 0; k < 16; ++k) Ys[k * kYStride + lane] = k < CC ? Y[k < CC ? k : 0] : 0.0f;
   }
   float fin[3] = {0.0f, 0.0f, 0.0f}, go[3] = {0.0f, 0.0f, 0.0f};
   if (inside) {
@@ -592,6 +650,7 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
   bool done = !inside;
   float tx0, tx1, ty0, ty1;
   tile_bounds(ctx, tx0, tx1, ty0, ty1);
+  const float4 blk = warp_block(px, py);
 
   for (int base = 0; base < n; base += B) {
     if (__syncthreads_and(done)) break;
@@ -599,10 +658,12 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
     for (int f = t; f < nb * NV; f += nthr) s_grad[f] = 0.0f;
     for (int j = t; j < nb; j += nthr) s_touched[j] = 0;
     const int nk =
-        load_batch<C>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1, s_wcount);
+        load_batch<C, true>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1, s_wcount);
+    const int nw = __all_sync(kFull, done) ? 0 : warp_list(L, nk, blk, wl, lane);
 
     int nslot = 0;  // warp-uniform: Gaussians staged in this warp's weight matrix
-    for (int i = 0; i < nk; ++i) {
+    for (int j = 0; j < nw; ++j) {
+      const int i = wl[j];
       if (__all_sync(kFull, done)) break;
       bool contrib = false;
       float sc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
@@ -635,7 +696,8 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
 #pragma unroll
               for (int ch = 0; ch < 3; ++ch) w[ch] = coeff * (y[ch] * (1.0f - y[ch])) * go[ch];
               const float one_m = fmaf(-al, G, 1.0f);
-              const float inv_one_m = 1.0f / one_m;
+              float inv_one_m;  // gradient path only: the hardware reciprocal (1 ulp)
+              asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv_one_m) : "f"(one_m));
               float P = 0.0f;
 #pragma unroll
               for (int ch = 0; ch < 3; ++ch) {
@@ -643,7 +705,7 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
                 P = fmaf(go[ch], fmaf(y[ch], T, -q), P);
               }
               const float dg = P * al * G;
-              const float inv_det = 1.0f / fmaf(cv.x, cv.w, -(cv.y * cv.z));
+              const float inv_det = L.inv_det[i];
               const float tmpx = fmaf(x, cv.w, -(yy * cv.z)) * inv_det;
               const float tmpy = fmaf(-x, cv.y, yy * cv.x) * inv_det;
               const float dx = dg * tmpx, dy = dg * tmpy;
@@ -701,24 +763,25 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
       } else if (idx == 5) {
         atomicAdd(a.g_alpha + id, val);
       } else {
-        const int e = idx - 6, ch = e / CC, k = e - ch * CC;
-        atomicAdd(ctx.g_sh + ((id - ctx.item_lo) * 3 + ch) * ctx.sh_stride + k, val);
+        const int e = idx - 6, ch = e / CSTR, k = e - ch * CSTR;
+        if (k < CC) atomicAdd(ctx.g_sh + ((id - ctx.item_lo) * 3 + ch) * ctx.sh_stride + k, val);
       }
     }
   }
 }
 
 template <int C>
-size_t fwd_smem(int B) {
-  return (size_t)B * (10 + Sh<C>::GSH) * sizeof(float);
+size_t fwd_smem(int B, int nthr) {
+  return (size_t)B * (kRecordFloats + Sh<C>::GSH) * sizeof(float) +
+         (size_t)(nthr / 32) * B * sizeof(int);
 }
 
 template <int C>
 size_t bwd_smem(int B, int nthr) {
-  constexpr int NV = 6 + 3 * Sh<C>::CC;
+  constexpr int NV = Grad<C>::NV;
   const int nwarps = nthr / 32;
-  return (size_t)B * (10 + Sh<C>::GSH + NV + 1) * sizeof(float) +
-         (size_t)nwarps * (16 * kWStride + 32 * kYStride + 8) * sizeof(float);
+  return (size_t)B * (kRecordFloats + Sh<C>::GSH + NV + 1) * sizeof(float) +
+         (size_t)nwarps * (16 * kWStride + 16 * kYStride + 8 + B) * sizeof(float);
 }
 
 inline int block_threads(const RasterArgs &a) { return (a.tile_w * a.tile_h + 31) / 32 * 32; }
@@ -740,7 +803,7 @@ template <int C, int MAXT, bool BATCHED>
 int launch_fwd_tt(RasterArgs a, int64_t grid, cudaStream_t s) {
   const int nthr = block_threads(a);
   a.batch = nthr < 128 ? nthr : 128;
-  const size_t smem = fwd_smem<C>(a.batch);
+  const size_t smem = fwd_smem<C>(a.batch, nthr);
   static size_t attr_done = 0;
   cudaError_t e = ensure_smem(raster_forward_kernel<C, MAXT, BATCHED>, smem, attr_done);
   if (e != cudaSuccess) return cuda_status(e, "raster_forward smem attribute");
