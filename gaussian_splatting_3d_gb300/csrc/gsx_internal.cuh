@@ -112,6 +112,7 @@ struct RasterArgs {
   // batched passes: per-view table in device memory (nullptr for one view)
   const gsx_batch_view *views;
   int32_t n_views;
+  int32_t vec_grads;  // g_mean2d 8-byte and g_cov2d 16-byte aligned (set by the launcher)
 };
 int launch_raster_forward(const RasterArgs &a, int C, cudaStream_t s);
 int launch_raster_backward(const RasterArgs &a, int C, cudaStream_t s);

@@ -480,9 +480,12 @@ __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a
         float y0 = fast_sigmoid(sh_logit<C>(s, Y2));
         float y1 = fast_sigmoid(sh_logit<C>(s + CCP, Y2));
         float y2 = fast_sigmoid(sh_logit<C>(s + 2 * CCP, Y2));
-        if (isnan(y0 * coeff)) y0 = 0.0f;
-        if (isnan(y1 * coeff)) y1 = 0.0f;
-        if (isnan(y2 * coeff)) y2 = 0.0f;
+        // coeff is finite here, so y * coeff is NaN exactly when y is; fmaxf
+        // returns its non-NaN operand and y >= 0, so this is the reference's
+        // `if isnan(y * coeff) y = 0`
+        y0 = fmaxf(y0, 0.0f);
+        y1 = fmaxf(y1, 0.0f);
+        y2 = fmaxf(y2, 0.0f);
         o0 = fmaf(coeff, y0, o0);
         o1 = fmaf(coeff, y1, o1);
         o2 = fmaf(coeff, y2, o2);
@@ -497,6 +500,18 @@ __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a
     dst[1] = o1;
     dst[2] = o2;
   }
+}
+
+// Vector reductions into global memory (red.global.add.v{2,4}.f32, sm_90+):
+// the address must be 8- / 16-byte aligned.
+__device__ __forceinline__ void red_add_v4(float *dst, float4 v) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst), "f"(v.x), "f"(v.y),
+               "f"(v.z), "f"(v.w)
+               : "memory");
+}
+
+__device__ __forceinline__ void red_add_v2(float *dst, float2 v) {
+  asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(dst), "f"(v.x), "f"(v.y) : "memory");
 }
 
 // Sum of six per-lane values over the warp: reduce-scatter over offsets 16,
@@ -543,14 +558,17 @@ constexpr int kYStride = 36;  // row stride of the basis, stored k-major: 16 row
                               // (conflict-free both for the per-pixel writes and the
                               // B-fragment reads: bank = 4 g + tq + const)
 
-// Per-Gaussian gradient record in shared memory: 6 scalars, then 3 SH
-// channels with a channel stride that keeps the three channels' atomics of
-// one mma fragment on distinct banks (20 for C = 4: windows 0-7, 20-27, 8-15).
+// Per-Gaussian gradient record in shared memory (NV floats, 16-byte
+// aligned): mean2d (0, 1), cov2d entries 0, 1 = 2, 3 (2, 3, 4), alpha (5),
+// two spare, then 3 SH channels from float kShOff with a channel stride that
+// keeps each channel 16-byte aligned and the three channels' atomics of one
+// mma fragment on distinct banks (20 for C = 4: windows 8-15, 28-35, 16-23).
+constexpr int kShOff = 8;
 template <int C>
 struct Grad {
   static constexpr int CC = C * C;
-  static constexpr int CSTR = CC == 16 ? 20 : CC;
-  static constexpr int NV = 6 + 3 * CSTR;
+  static constexpr int CSTR = CC == 16 ? 20 : (CC + 3) & ~3;
+  static constexpr int NV = kShOff + 3 * CSTR;
 };
 
 // SH gradients of the staged Gaussians: D[r][k] = sum_p W[r][p] * Y[p][k] for
@@ -591,7 +609,7 @@ __device__ __forceinline__ void flush_sh_group(const float *Ws, const float *Ys,
       const int k = 8 * nt + 2 * tq + (e & 1);
       if (r < rows && k < CC && d[nt][e] != 0.0f) {
         const int slot = r / 3, ch = r - 3 * slot;
-        atomicAdd(&s_grad[slots[slot] * NV + 6 + ch * CSTR + k], d[nt][e]);
+        atomicAdd(&s_grad[slots[slot] * NV + kShOff + ch * CSTR + k], d[nt][e]);
       }
     }
 }
@@ -689,8 +707,7 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
               float y[3];
 #pragma unroll
               for (int ch = 0; ch < 3; ++ch) {
-                y[ch] = fast_sigmoid(sh_logit<C>(s + ch * CCP, Y2));
-                if (isnan(y[ch] * coeff)) y[ch] = 0.0f;
+                y[ch] = fmaxf(fast_sigmoid(sh_logit<C>(s + ch * CCP, Y2)), 0.0f);  // NaN -> 0
                 o[ch] = fmaf(coeff, y[ch], o[ch]);
               }
 #pragma unroll
@@ -745,26 +762,51 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
     }
     if (!done && T < thr) done = true;
     __syncthreads();
-    for (int f = t; f < nk * NV; f += nthr) {
-      const int j = f / NV, idx = f - j * NV;
+    // one vector reduction per chunk of a touched Gaussian's record: mean2d
+    // (v2), cov2d (v4, entries 1 and 2 both get dL/dcov01 as the reference
+    // writes them), alpha, and the SH channels in 4-float chunks
+    constexpr int NCH = Grad<C>::CSTR / 4;
+    constexpr int NCHUNK = 3 + 3 * NCH;
+    for (int f = t; f < nk * NCHUNK; f += nthr) {
+      const int j = f / NCHUNK, c = f - j * NCHUNK;
       if (!s_touched[j]) continue;
-      const float val = s_grad[f];
-      if (val == 0.0f) continue;
+      const float *rec = s_grad + j * NV;
       const int64_t id = L.ids[j];
-      if (idx < 2) {
-        atomicAdd(a.g_mean2d + 2 * id + idx, val);
-      } else if (idx == 2) {
-        atomicAdd(a.g_cov2d + 4 * id, val);
-      } else if (idx == 3) {
-        atomicAdd(a.g_cov2d + 4 * id + 1, val);
-        atomicAdd(a.g_cov2d + 4 * id + 2, val);
-      } else if (idx == 4) {
-        atomicAdd(a.g_cov2d + 4 * id + 3, val);
-      } else if (idx == 5) {
-        atomicAdd(a.g_alpha + id, val);
+      if (c == 0) {
+        const float2 v = *reinterpret_cast<const float2 *>(rec);
+        if (a.vec_grads) {
+          if (v.x != 0.0f || v.y != 0.0f) red_add_v2(a.g_mean2d + 2 * id, v);
+        } else {
+          if (v.x != 0.0f) atomicAdd(a.g_mean2d + 2 * id, v.x);
+          if (v.y != 0.0f) atomicAdd(a.g_mean2d + 2 * id + 1, v.y);
+        }
+      } else if (c == 1) {
+        const float4 v = make_float4(rec[2], rec[3], rec[3], rec[4]);
+        if (a.vec_grads) {
+          if (v.x != 0.0f || v.y != 0.0f || v.w != 0.0f) red_add_v4(a.g_cov2d + 4 * id, v);
+        } else {
+          if (v.x != 0.0f) atomicAdd(a.g_cov2d + 4 * id, v.x);
+          if (v.y != 0.0f) {
+            atomicAdd(a.g_cov2d + 4 * id + 1, v.y);
+            atomicAdd(a.g_cov2d + 4 * id + 2, v.y);
+          }
+          if (v.w != 0.0f) atomicAdd(a.g_cov2d + 4 * id + 3, v.w);
+        }
+      } else if (c == 2) {
+        if (rec[5] != 0.0f) atomicAdd(a.g_alpha + id, rec[5]);
       } else {
-        const int e = idx - 6, ch = e / CSTR, k = e - ch * CSTR;
-        if (k < CC) atomicAdd(ctx.g_sh + ((id - ctx.item_lo) * 3 + ch) * ctx.sh_stride + k, val);
+        const int e = c - 3, ch = e / NCH, k = 4 * (e - ch * NCH);
+        const float4 v = *reinterpret_cast<const float4 *>(rec + kShOff + ch * Grad<C>::CSTR + k);
+        if (v.x == 0.0f && v.y == 0.0f && v.z == 0.0f && v.w == 0.0f) continue;
+        float *dst = ctx.g_sh + ((id - ctx.item_lo) * 3 + ch) * ctx.sh_stride + k;
+        if (k + 4 <= CC && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+          red_add_v4(dst, v);
+        } else {
+          const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (k + q < CC && vv[q] != 0.0f) atomicAdd(dst + q, vv[q]);
+        }
       }
     }
   }
@@ -821,6 +863,10 @@ int launch_fwd_t(const RasterArgs &a, int64_t grid, cudaStream_t s) {
 template <int C, int MAXT, bool BATCHED>
 int launch_bwd_tt(RasterArgs a, int64_t grid, cudaStream_t s) {
   const int nthr = block_threads(a);
+  a.vec_grads = ((reinterpret_cast<uintptr_t>(a.g_mean2d) & 7) == 0 &&
+                 (reinterpret_cast<uintptr_t>(a.g_cov2d) & 15) == 0)
+                    ? 1
+                    : 0;
   a.batch = nthr < 64 ? nthr : 64;
   const size_t smem = bwd_smem<C>(a.batch, nthr);
   static size_t attr_done = 0;
