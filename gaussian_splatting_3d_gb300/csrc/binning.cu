@@ -235,7 +235,11 @@ __device__ __forceinline__ long long rect_count(const int32_t *tl, const int32_t
 
 // Exclusive scan of key counts in depth order (decoupled look-back over
 // chunks of 2048 Gaussians) fused with the emission of (tile, Gaussian)
-// pairs.  The last chunk writes the key total.
+// pairs.  Warp w of a chunk owns its items w*256 + j*32 + lane (j = 0..7), so
+// item loads are coalesced; per group j the warp scans the 32 counts and then
+// writes the group's keys cooperatively, lane l taking keys l, l+32, ... of
+// the group (the owner item found by a 5-step search), so key writes are
+// coalesced too.  The last chunk writes the key total.
 __global__ void __launch_bounds__(kThreads)
     emit_kernel(const uint32_t *__restrict__ order, uint32_t n,
                 const int32_t *__restrict__ rect_tl, const int32_t *__restrict__ rect_br,
@@ -248,17 +252,21 @@ __global__ void __launch_bounds__(kThreads)
   __shared__ unsigned long long s_tmp[kWarps];
   __shared__ unsigned long long s_prefix;
   __shared__ uint32_t s_chunk;
-  const int t = threadIdx.x;
+  // staging of one 32-item group per warp
+  __shared__ unsigned long long s_excl[kWarps][32];
+  __shared__ uint32_t s_g[kWarps][32], s_tb[kWarps][32];
+  __shared__ int32_t s_x0[kWarps][32], s_y0[kWarps][32], s_w[kWarps][32], s_ntw[kWarps][32];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   if (t == 0) s_chunk = atomicAdd(chunk_counter, 1u);
   __syncthreads();
   const uint32_t chunk = s_chunk;
-  const uint32_t first = chunk * (uint32_t)kEmitTile + t * kEmitItems;
+  const uint32_t first = chunk * (uint32_t)kEmitTile + (uint32_t)w * (32 * kEmitItems) + lane;
   uint32_t gid[kEmitItems];
   long long cnt[kEmitItems];
   unsigned long long mysum = 0;
 #pragma unroll
   for (int j = 0; j < kEmitItems; ++j) {
-    const uint32_t idx = first + j;
+    const uint32_t idx = first + 32u * j;
     gid[j] = 0;
     cnt[j] = 0;
     if (idx < n) {
@@ -275,9 +283,18 @@ __global__ void __launch_bounds__(kThreads)
       mysum += (unsigned long long)c;
     }
   }
-  unsigned long long block_total;
-  const unsigned long long excl =
-      block_exclusive_scan<unsigned long long>(mysum, s_tmp, &block_total);
+  // warp totals -> offsets of the warps within the chunk, chunk total
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mysum += __shfl_xor_sync(0xffffffffu, mysum, o);
+  if (lane == 0) s_tmp[w] = mysum;
+  __syncthreads();
+  unsigned long long warp_off = 0, block_total = 0;
+#pragma unroll
+  for (int k = 0; k < kWarps; ++k) {
+    const unsigned long long c = s_tmp[k];
+    if (k < w) warp_off += c;
+    block_total += c;
+  }
   if (t == 0) {
     unsigned long long prev = 0;
     unsigned long long *mine = status + chunk;
@@ -312,41 +329,78 @@ __global__ void __launch_bounds__(kThreads)
     }
   }
   __syncthreads();
-  unsigned long long off = s_prefix + excl;
-#pragma unroll 1
+  unsigned long long gbase = s_prefix + warp_off;  // first key of the current group
+#pragma unroll
   for (int j = 0; j < kEmitItems; ++j) {
-    if (cnt[j] == 0) continue;
-    const uint32_t g = gid[j];
-    const int32_t *tl = rect_tl + (size_t)g * rect_stride;
-    const int32_t *br = rect_br + (size_t)g * rect_stride;
-    if (rect_count(tl, br) != cnt[j]) atomicOr(error, kErrCount);
-    // tiles of this item's image: one image, or the item's view in a batch
-    int32_t ntw = n_tiles_w, nth = n_tiles_h;
-    uint32_t tile_base = 0;
-    if (views) {
-      int lo = 0, hi = n_views - 1;
-      while (lo < hi) {
+    // group scan: exclusive offsets of the 32 items, group total
+    unsigned long long x = (unsigned long long)cnt[j];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    const unsigned long long gtotal = __shfl_sync(0xffffffffu, x, 31);
+    const unsigned long long excl = x - (unsigned long long)cnt[j];
+    int32_t x0 = 0, y0 = 0, wd = 1, ntw = n_tiles_w;
+    uint32_t tile_base = 0xffffffffu;  // all ones: the item lies outside its tile grid
+    if (cnt[j] > 0) {
+      const uint32_t g = gid[j];
+      const int32_t *tl = rect_tl + (size_t)g * rect_stride;
+      const int32_t *br = rect_br + (size_t)g * rect_stride;
+      if (rect_count(tl, br) != cnt[j]) atomicOr(error, kErrCount);
+      // tiles of this item's image: one image, or the item's view in a batch
+      int32_t nth = n_tiles_h;
+      uint32_t tb = 0;
+      if (views) {
+        int lo = 0, hi = n_views - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (views[mid].item_offset <= (int64_t)g) lo = mid;
+          else hi = mid - 1;
+        }
+        ntw = views[lo].n_tiles_w;
+        nth = views[lo].n_tiles_h;
+        tb = (uint32_t)views[lo].tile_offset;
+      }
+      const bool in_grid = tl[0] >= 0 && tl[1] >= 0 && br[0] < ntw && br[1] < nth;
+      if (!in_grid) atomicOr(error, kErrRange);
+      else tile_base = tb;
+      x0 = tl[0];
+      y0 = tl[1];
+      wd = max(br[0] - tl[0] + 1, 1);
+    }
+    s_excl[w][lane] = excl;
+    s_g[w][lane] = gid[j];
+    s_tb[w][lane] = tile_base;
+    s_x0[w][lane] = x0;
+    s_y0[w][lane] = y0;
+    s_w[w][lane] = wd;
+    s_ntw[w][lane] = ntw;
+    __syncwarp();
+    // keys [gbase, gbase + gtotal) of which those below the capacity are written
+    const unsigned long long lim =
+        gbase >= capacity ? 0ull : (gtotal < capacity - gbase ? gtotal : capacity - gbase);
+    for (unsigned long long q = lane; q < lim; q += 32) {
+      int lo = 0, hi = 31;
+#pragma unroll
+      for (int step = 0; step < 5; ++step) {
         const int mid = (lo + hi + 1) >> 1;
-        if (views[mid].item_offset <= (int64_t)g) lo = mid;
+        if (s_excl[w][mid] <= q) lo = mid;
         else hi = mid - 1;
       }
-      ntw = views[lo].n_tiles_w;
-      nth = views[lo].n_tiles_h;
-      tile_base = (uint32_t)views[lo].tile_offset;
+      const uint32_t local = (uint32_t)(q - s_excl[w][lo]);
+      const uint32_t wdt = (uint32_t)s_w[w][lo];
+      const uint32_t ry = local / wdt, rx = local - ry * wdt;
+      const uint32_t tb = s_tb[w][lo];
+      const unsigned long long pos = gbase + q;
+      tile_out[pos] = tb == 0xffffffffu
+                          ? 0xffffffffu
+                          : tb + (uint32_t)(((int32_t)ry + s_y0[w][lo]) * s_ntw[w][lo] +
+                                            ((int32_t)rx + s_x0[w][lo]));
+      id_out[pos] = s_g[w][lo];
     }
-    const bool in_grid = tl[0] >= 0 && tl[1] >= 0 && br[0] < ntw && br[1] < nth;
-    if (!in_grid) atomicOr(error, kErrRange);
-    if (off >= capacity) break;  // the count is known from the scan; nothing more fits
-    const unsigned long long stop =
-        off + (unsigned long long)cnt[j] < capacity ? off + (unsigned long long)cnt[j] : capacity;
-    for (int32_t y = tl[1]; y <= br[1] && off < stop; ++y)
-      for (int32_t x = tl[0]; x <= br[0] && off < stop; ++x) {
-        tile_out[off] = in_grid ? tile_base + (uint32_t)(y * ntw + x) : 0xffffffffu;
-        id_out[off] = g;
-        ++off;
-      }
-    off = s_prefix + excl;  // recompute the running offset from the counts
-    for (int jj = 0; jj <= j; ++jj) off += (unsigned long long)cnt[jj];
+    __syncwarp();
+    gbase += gtotal;
   }
 }
 
