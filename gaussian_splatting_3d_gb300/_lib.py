@@ -130,6 +130,12 @@ SIGNATURES = {
     "gsx_batch_render_forward": (c_int, [P, P, c_int32, c_int64] + [P] * 6 + [c_float, P]),
     "gsx_batch_render_backward": (c_int, [P, P, c_int32, c_int64] + [P] * 9 + [c_float, P]),
     "gsx_batch_project_backward": (c_int, [P, P, c_int32] + [P] * 4 + [c_int32, P]),
+    # adaptive density control
+    "gsx_densify_count_visible": (c_int, [c_int64, P, P, P]),
+    "gsx_densify_accumulate": (c_int, [c_int64, P, c_int32, P, P, c_int32, P]),
+    "gsx_densify_classify": (c_int, [c_int64, P, P, P, c_float, c_float, c_int32, P, P]),
+    "gsx_densify_rewrite": (c_int, [c_int64, P, P, P, P, c_int64, c_int64, c_int64, P, P, P, P, c_int32, P,
+                                    c_float, ctypes.c_uint64, P, P, P, P, P, P]),
 }
 
 _lib = None

@@ -69,6 +69,15 @@ class Scene:
         return int(self.mean.shape[0])
 
     @classmethod
+    def from_checkpoint(cls, path, device) -> "Scene":
+        """A scene from an SHRenderer checkpoint (gs/sh_renderer.py:663-679)."""
+        from .checkpoint import load_state
+
+        sd = load_state(path, device)
+        return cls(sd["mean"], sd["qvec"], sd["svec_before_activation"], sd["sh_coeffs"],
+                   sd["alpha_before_activation"])
+
+    @classmethod
     def from_arrays(cls, sc, device) -> "Scene":
         return cls(*(torch.from_numpy(np.ascontiguousarray(a)).to(device) for a in
                      (sc.mean, sc.qvec, sc.log_scale, sc.sh, sc.alpha_logit)))
@@ -98,9 +107,12 @@ class BatchPipeline:
         self.views = views
         self.backward_enabled = backward
         V = len(views)
-        C = sh_order or st.sh_order or int(round(scenes[0].sh.shape[-1] ** 0.5))
+        used = {v.scene for v in views}
+        if any(scenes[i] is None for i in used):
+            raise ValueError("a view refers to a scene that is not resident")
+        C = sh_order or st.sh_order or int(round(scenes[views[0].scene].sh.shape[-1] ** 0.5))
         self.C = C
-        for s in scenes:
+        for s in (scenes[i] for i in sorted(used)):
             for t, name in ((s.mean, "mean"), (s.qvec, "qvec"), (s.log_scale, "log_scale"), (s.sh, "sh"),
                             (s.alpha_logit, "alpha_logit")):
                 check_tensor(t, name)

@@ -396,4 +396,55 @@ int gsx_project_backward(int64_t n, const float *mean, const float *qvec,
                                  grad_log_scale, grad_alpha_logit, grad_flags, as_stream(stream));
 }
 
+
+// ---------------------------------------------------------------- densify
+int gsx_densify_count_visible(int64_t n, const int32_t *counts, int32_t *cnt, void *stream) {
+  g_err[0] = 0;
+  GSX_REQUIRE(n >= 0, "n must be >= 0");
+  GSX_REQUIRE(n == 0 || (counts && cnt), "null pointer argument");
+  return launch_count_visible(n, counts, cnt, as_stream(stream));
+}
+
+int gsx_densify_accumulate(int64_t n, const float *grad, int32_t dim, const int32_t *counts,
+                           float *grad_accum, int32_t reduce_max, void *stream) {
+  g_err[0] = 0;
+  GSX_REQUIRE(n >= 0, "n must be >= 0");
+  GSX_REQUIRE(dim == 2 || dim == 3, "dim must be 2 or 3 (got %d)", dim);
+  GSX_REQUIRE(n == 0 || (grad && grad_accum), "null pointer argument");
+  return launch_accumulate_norm(n, grad, dim, counts, grad_accum, reduce_max ? 1 : 0,
+                                as_stream(stream));
+}
+
+int gsx_densify_classify(int64_t n, const float *grad_accum, const int32_t *cnt,
+                         const float *log_scale, float grad_thresh, float scale_thresh,
+                         int32_t divide_by_count, uint8_t *cls, void *stream) {
+  g_err[0] = 0;
+  GSX_REQUIRE(n >= 0, "n must be >= 0");
+  GSX_REQUIRE(n == 0 || (grad_accum && log_scale && cls && (cnt || !divide_by_count)),
+              "null pointer argument");
+  return launch_classify(n, grad_accum, cnt, log_scale, grad_thresh, scale_thresh,
+                         divide_by_count ? 1 : 0, cls, as_stream(stream));
+}
+
+int gsx_densify_rewrite(int64_t n, const uint8_t *cls, const int64_t *pos_stay,
+                        const int64_t *pos_clone, const int64_t *pos_split, int64_t n_stay,
+                        int64_t n_clone, int64_t n_split, const float *mean, const float *qvec,
+                        const float *log_scale, const float *sh, int32_t sh_len,
+                        const float *alpha_logit, float shrink, uint64_t seed, float *out_mean,
+                        float *out_qvec, float *out_log_scale, float *out_sh, float *out_alpha_logit,
+                        void *stream) {
+  g_err[0] = 0;
+  GSX_REQUIRE(n >= 0 && n_stay >= 0 && n_clone >= 0 && n_split >= 0, "negative size");
+  GSX_REQUIRE(n_stay + n_split == n, "every Gaussian either stays or is split");
+  GSX_REQUIRE(sh_len > 0, "sh_len must be positive");
+  GSX_REQUIRE(shrink > 0.0f, "shrink factor must be positive");
+  GSX_REQUIRE(n == 0 || (cls && pos_stay && pos_clone && pos_split && mean && qvec && log_scale &&
+                         sh && alpha_logit && out_mean && out_qvec && out_log_scale && out_sh &&
+                         out_alpha_logit),
+              "null pointer argument");
+  return launch_rewrite(n, cls, pos_stay, pos_clone, pos_split, n_stay, n_clone, n_split, mean,
+                        qvec, log_scale, sh, sh_len, alpha_logit, logf(shrink), seed, out_mean,
+                        out_qvec, out_log_scale, out_sh, out_alpha_logit, as_stream(stream));
+}
+
 }  // extern "C"

@@ -95,6 +95,20 @@ int launch_project_backward_batch(const gsx_batch_view *views, int32_t n_views, 
                                   const float *g_cov2d, const float *g_alpha, int32_t flags,
                                   cudaStream_t s);
 
+// Adaptive density control (densify.cu).
+int launch_count_visible(int64_t n, const int32_t *counts, int32_t *cnt, cudaStream_t s);
+int launch_accumulate_norm(int64_t n, const float *grad, int dim, const int32_t *counts,
+                           float *accum, int reduce_max, cudaStream_t s);
+int launch_classify(int64_t n, const float *accum, const int32_t *cnt, const float *log_scale,
+                    float grad_thresh, float scale_thresh, int divide_by_count, uint8_t *cls,
+                    cudaStream_t s);
+int launch_rewrite(int64_t n, const uint8_t *cls, const int64_t *pos_stay, const int64_t *pos_clone,
+                   const int64_t *pos_split, int64_t n_stay, int64_t n_clone, int64_t n_split,
+                   const float *mean, const float *qvec, const float *log_scale, const float *sh,
+                   int sh_len, const float *alpha_logit, float log_shrink, uint64_t seed,
+                   float *o_mean, float *o_qvec, float *o_log_scale, float *o_sh, float *o_alpha,
+                   cudaStream_t s);
+
 struct RasterArgs {
   int64_t n, n_keys;  // Gaussians and list entries: bounds for start/end/ids
   int32_t width, height, tile_w, tile_h, n_tiles_w, n_tiles_h;

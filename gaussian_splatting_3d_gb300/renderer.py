@@ -264,11 +264,14 @@ class ViewPipeline:
         # keep the capacity near 1.25 K so the sort grids stay small
         if K * 2 < self.key_capacity:
             self.key_capacity = max(int(K * 1.25) + 4096, 1 << 16)
+        visible_counts = pr.counts
         if settings.recompute_projection:
+            visible_counts = pr.counts.clone()
             pr = None
             _bin_buffers(dev).release()
         return dict(pr=pr, ids=ids, start=start, end=end, K=K, cap=cap, topleft=topleft, c2w_dev=c2w_dev,
-                    out=out, params=params, gcam=gcam, grad_flags=settings.grad_flags(), settings=settings)
+                    out=out, params=params, gcam=gcam, grad_flags=settings.grad_flags(), settings=settings,
+                    counts=visible_counts)
 
     def backward(self, state, mean, qvec, log_scale, sh, alpha_logit, grad_out, timer=None):
         dev = mean.device
@@ -296,6 +299,7 @@ class ViewPipeline:
             _lib.call("gsx_project_backward", n, ptr(mean), ptr(qvec), ptr(log_scale), ptr(alpha_logit),
                       ctypes.byref(state["gcam"]), ptr(pr.counts), ptr(g_mean2d), ptr(g_cov2d), ptr(g_alpha),
                       ptr(g_mean), ptr(g_q), ptr(g_ls), ptr(g_al), state["grad_flags"], stream_handle(dev))
+        state["g_mean2d"] = g_mean2d  # dL/dmean2d (normalised image coordinates), for densification
         return g_mean, g_q, g_ls, g_sh, g_al
 
 
@@ -351,7 +355,7 @@ def _pipeline(device) -> ViewPipeline:
 
 class FusedRender(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, mean, qvec, log_scale, sh, alpha_logit, c2w_np, cam, settings):
+    def forward(ctx, mean, qvec, log_scale, sh, alpha_logit, c2w_np, cam, settings, aux=None):
         for x, name in ((mean, "mean"), (qvec, "qvec"), (log_scale, "log_scale"), (sh, "sh_coeffs"),
                         (alpha_logit, "alpha_logit")):
             check_tensor(x, name)
@@ -360,24 +364,31 @@ class FusedRender(torch.autograd.Function):
         ctx.save_for_backward(mean, qvec, log_scale, sh, alpha_logit)
         ctx.state = state
         ctx.pipe = pipe
+        ctx.aux = aux
+        if aux is not None:  # per-Gaussian key counts of this view (0 = culled)
+            aux["counts"] = state["counts"]
         return state["out"]
 
     @staticmethod
     def backward(ctx, grad_out):
         mean, qvec, log_scale, sh, alpha_logit = ctx.saved_tensors
         grads = ctx.pipe.backward(ctx.state, mean, qvec, log_scale, sh, alpha_logit, grad_out)
+        if ctx.aux is not None:
+            ctx.aux["mean2d_grad"] = ctx.state["g_mean2d"]
         ctx.state = None
-        return grads + (None, None, None)
+        return grads + (None, None, None, None)
 
 
 def rasterize(mean, qvec, log_scale, sh_coeffs, alpha_logit, c2w, cam: CameraInfo,
-              settings: RasterSettings | None = None) -> torch.Tensor:
+              settings: RasterSettings | None = None, aux: dict | None = None) -> torch.Tensor:
     """Render one view: parameters as in SHRenderer (log-scales, opacity
     logits, SH [N,3,C_max^2]) and a [3,4] camera-to-world (host array or
     tensor).  Returns the [H,W,3] image; differentiable w.r.t. all five
-    parameter tensors."""
+    parameter tensors.  With an ``aux`` dict, the forward stores the
+    per-Gaussian key counts (``aux["counts"]``, 0 = culled) and the backward
+    dL/dmean2d (``aux["mean2d_grad"]``, [N,2]) for adaptive density control."""
     settings = settings or RasterSettings()
     if isinstance(c2w, torch.Tensor):
         c2w = c2w.detach().to("cpu", torch.float32).numpy()
     return FusedRender.apply(mean, qvec, log_scale, sh_coeffs, alpha_logit, np.asarray(c2w, np.float32), cam,
-                             settings)
+                             settings, aux)

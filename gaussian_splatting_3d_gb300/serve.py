@@ -113,8 +113,7 @@ class RenderServer:
         self.scenes = list(scenes)
         self.settings = settings or RasterSettings()
         self.budget = int(budget_bytes)
-        self.resident = sum(t.numel() * t.element_size() for s in self.scenes
-                            for t in (s.mean, s.qvec, s.log_scale, s.sh, s.alpha_logit))
+        self.resident = sum(self._scene_bytes(s) for s in self.scenes)
         if self.resident > self.budget:
             raise ValueError(f"the resident scenes ({self.resident} bytes) exceed the memory budget")
         self.sh_orders = [int(round(s.sh.shape[-1] ** 0.5)) if self.settings.sh_order is None
@@ -138,9 +137,48 @@ class RenderServer:
         self._next_rid = 0
         self._lib = _lib.load()
 
+    # ---------------------------------------------------------------- scenes
+    @staticmethod
+    def _scene_bytes(s: Scene) -> int:
+        return sum(t.numel() * t.element_size() for t in (s.mean, s.qvec, s.log_scale, s.sh, s.alpha_logit))
+
+    def add_scene(self, scene: Scene | str) -> int:
+        """Make a scene resident (a Scene or the path of an SHRenderer
+        checkpoint); returns its index.  Refused when it does not fit the
+        memory budget next to the resident scenes and the batches in flight."""
+        if not isinstance(scene, Scene):
+            scene = Scene.from_checkpoint(scene, self.device)
+        need = self._scene_bytes(scene)
+        if self.resident + self.reserved + need > self.budget:
+            raise MemoryError(f"scene of {need} bytes does not fit the memory budget")
+        self.resident += need
+        C = int(round(scene.sh.shape[-1] ** 0.5)) if self.settings.sh_order is None else self.settings.sh_order
+        for i, s in enumerate(self.scenes):  # reuse a freed slot
+            if s is None:
+                self.scenes[i] = scene
+                self.sh_orders[i] = C
+                return i
+        self.scenes.append(scene)
+        self.sh_orders.append(C)
+        return len(self.scenes) - 1
+
+    def remove_scene(self, index: int) -> None:
+        """Release a resident scene that no waiting or running request uses."""
+        s = self.scenes[index]
+        if s is None:
+            raise IndexError(f"scene {index} is not resident")
+        busy = any(r.scene == index for r in self.waiting) or any(
+            r.scene == index for b in self.in_flight for r in b.requests)
+        if busy:
+            raise RuntimeError(f"scene {index} has requests waiting or in flight")
+        self.resident -= self._scene_bytes(s)
+        self.scenes[index] = None
+        for key in [k for k in self.keys_per_gaussian if k[0] == index]:
+            del self.keys_per_gaussian[key]
+
     # -------------------------------------------------------------- requests
     def submit(self, scene: int, c2w, cam: CameraInfo, t_arrival: float | None = None) -> Request:
-        if not 0 <= scene < len(self.scenes):
+        if not 0 <= scene < len(self.scenes) or self.scenes[scene] is None:
             raise IndexError(f"scene {scene} is not resident")
         req = Request(scene, np.asarray(c2w, np.float32), cam)
         req.rid = self._next_rid

@@ -340,6 +340,39 @@ int gsx_project_backward(int64_t n, const float *mean, const float *qvec,
                          float *grad_qvec, float *grad_log_scale,
                          float *grad_alpha_logit, int32_t grad_flags, void *stream);
 
+
+/*
+ * Adaptive density control (no reference counterpart at this boundary: the
+ * reference does these steps with torch ops in gs/sh_renderer.py:216,
+ * 426-540, 602-623).
+ *   gsx_densify_count_visible: cnt[i] += 1 where counts[i] > 0 (i.e. Gaussian
+ *     i survived frustum culling in the last projection).
+ *   gsx_densify_accumulate: grad_accum[i] = max(grad_accum[i], |grad[i]|)
+ *     (reduce_max) or += |grad[i]|, grad f32[n,dim] (dim 3: dL/dmean, dim 2:
+ *     dL/dmean2d); with counts, only where counts[i] > 0.
+ *   gsx_densify_classify: cls[i] = 0 keep, 1 clone, 2 split: the statistic
+ *     (divided by cnt + 1e-5 when divide_by_count) above grad_thresh, split
+ *     when any exp(log_scale) > scale_thresh.
+ *   gsx_densify_rewrite: the new arrays [not split, in order] ++ [clones] ++
+ *     [split samples: copy 0 of every split Gaussian, then copy 1], from the
+ *     exclusive prefix counts of (cls != 2), (cls == 1), (cls == 2); a split
+ *     sample is mean + R(q)^T (n * scale), n ~ N(0,1) from a counter-based
+ *     generator keyed by seed, with log-scale log(scale / shrink).
+ */
+int gsx_densify_count_visible(int64_t n, const int32_t *counts, int32_t *cnt, void *stream);
+int gsx_densify_accumulate(int64_t n, const float *grad, int32_t dim, const int32_t *counts,
+                           float *grad_accum, int32_t reduce_max, void *stream);
+int gsx_densify_classify(int64_t n, const float *grad_accum, const int32_t *cnt,
+                         const float *log_scale, float grad_thresh, float scale_thresh,
+                         int32_t divide_by_count, uint8_t *cls, void *stream);
+int gsx_densify_rewrite(int64_t n, const uint8_t *cls, const int64_t *pos_stay,
+                        const int64_t *pos_clone, const int64_t *pos_split, int64_t n_stay,
+                        int64_t n_clone, int64_t n_split, const float *mean, const float *qvec,
+                        const float *log_scale, const float *sh, int32_t sh_len,
+                        const float *alpha_logit, float shrink, uint64_t seed, float *out_mean,
+                        float *out_qvec, float *out_log_scale, float *out_sh, float *out_alpha_logit,
+                        void *stream);
+
 #ifdef __cplusplus
 }
 #endif

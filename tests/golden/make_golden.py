@@ -196,6 +196,64 @@ def cases():
     return out
 
 
+def densify_fixture(gs_mod):
+    """The reference's adaptive density control (gs/sh_renderer.py:426-623)
+    on a small scene: update_grads for both statistics and reductions, then
+    split/clone (torch seed 0) and the low-opacity prune.  Gradient norms are
+    drawn well away from the threshold so rounding cannot flip a decision."""
+    from gaussian_splatting_3d_gb300 import scene as S
+    from gs.sh_renderer import SHRenderer
+
+    sc = S.custom_workload(400, 64, 64, 3, seed=21).scene
+    n = sc.n
+    g = torch.Generator().manual_seed(5)
+    thresh = 2e-4
+    dirs3 = torch.nn.functional.normalize(torch.randn(n, 3, generator=g), dim=-1)
+    dirs2 = torch.nn.functional.normalize(torch.randn(n, 2, generator=g), dim=-1)
+    mag = torch.where(torch.rand(n, generator=g) < 0.3, 4.0 * thresh, 0.25 * thresh)
+    mag = mag * (1.0 + torch.rand(n, generator=g))
+    G3 = (dirs3 * mag[:, None]).float()
+    G2 = (dirs2 * mag.flip(0)[:, None]).float()
+    vis = torch.rand(n, generator=g) < 0.8
+    gm0 = (torch.rand(n, generator=g) * 0.5 * thresh).float()
+    cnt0 = torch.randint(0, 3, (n,), generator=g, dtype=torch.int32)
+    log_s = torch.from_numpy(sc.log_scale.copy())
+    log_s[::3] += 1.5  # some large Gaussians: split rather than clone
+    out = dict(mean=sc.mean, qvec=sc.qvec, log_scale=log_s.numpy(), sh=sc.sh, alpha_logit=sc.alpha_logit,
+               G3=G3.numpy(), G2=G2.numpy(), vis=vis.numpy(), gm0=gm0.numpy(), cnt0=cnt0.numpy(),
+               thresh=np.float32(thresh), scale_thresh=np.float32(0.05), shrink=np.float32(1.6))
+    for split_type in ("mean_grad", "2d_mean_grad"):
+        for red in ("max", "mean"):
+            cfg = reference_cfg(4, 16)
+            cfg.update(split_type=split_type, split_reduction=red, pos_grad_thresh=thresh,
+                       split_scale_thresh=0.05, scale_shrink_factor=1.6, alpha_thresh=0.3)
+            r = SHRenderer(cfg)
+            r.N = n
+            r.mean = torch.nn.Parameter(torch.from_numpy(sc.mean.copy()))
+            r.qvec = torch.nn.Parameter(torch.from_numpy(sc.qvec.copy()))
+            r.svec_before_activation = torch.nn.Parameter(log_s.clone())
+            r.sh_coeffs = torch.nn.Parameter(torch.from_numpy(sc.sh.copy()))
+            r.alpha_before_activation = torch.nn.Parameter(torch.from_numpy(sc.alpha_logit.copy()))
+            r.grad_mean = gm0.clone()
+            r.cnt = cnt0.clone()
+            r.mean.grad = G3.clone()
+            r.frustum_culling_mask = vis.clone()
+            r.mean_2d = G2[vis].clone().requires_grad_(True)
+            r.mean_2d.grad = G2[vis].clone()
+            r.update_grads()
+            tag = f"{split_type}_{red}"
+            out[f"grad_mean_{tag}"] = r.grad_mean.numpy().copy()
+            torch.manual_seed(0)
+            r.split_gaussians()
+            out[f"split_{tag}_N"] = np.int64(r.N)
+            for k in ("mean", "qvec", "svec_before_activation", "sh_coeffs", "alpha_before_activation"):
+                out[f"split_{tag}_{k}"] = getattr(r, k).data.numpy().copy()
+            r.remove_low_alpha_gaussians()
+            out[f"prune_{tag}_N"] = np.int64(r.N)
+            out[f"prune_{tag}_mean"] = r.mean.data.numpy().copy()
+    return out
+
+
 def main():
     if not build_ref.reference_available():
         raise SystemExit("the reference sources are needed to generate fixtures")
@@ -206,6 +264,10 @@ def main():
     sys.path.insert(0, str(REF))
     torch.set_num_threads(8)
     only = set(sys.argv[1:])  # optional: names of the fixtures to (re)generate
+    if not only or "densify_400" in only:
+        fix = densify_fixture(gs_mod)
+        np.savez_compressed(HERE / "densify_400.npz", **fix)
+        print("densify_400.npz:", {k: int(v) for k, v in fix.items() if k.endswith("_N")})
     for name, wl, now_C in cases():
         if only and name not in only:
             continue

@@ -149,3 +149,27 @@ def test_poisson_stream_smoke():
     st = serve.latency_stats(reqs)
     assert len(reqs) == 16 and all(r.state == "done" for r in reqs)
     assert 0 < st["p50_ms"] <= st["p99_ms"] and wall > 0
+
+
+def test_scenes_from_checkpoints_added_and_removed(tmp_path):
+    from gaussian_splatting_3d_gb300 import checkpoint as ck
+
+    scenes = make_scenes(seed=130)
+    paths = []
+    for i, sc in enumerate(scenes):
+        paths.append(tmp_path / f"scene{i}.pt")
+        ck.save_state(paths[-1], sc.mean, sc.qvec, sc.log_scale, sc.sh, sc.alpha_logit, cfg={"i": i})
+    srv = serve.RenderServer([], dev(), budget_bytes=1e9)
+    idx = [srv.add_scene(str(p)) for p in paths]
+    assert idx == [0, 1, 2]
+    reqs = [srv.submit(*r) for r in make_requests(9, 3, seed=8)]
+    srv.drain()
+    for r in reqs:
+        np.testing.assert_array_equal(r.image.cpu().numpy(), alone(scenes[r.scene], r.c2w, r.cam).cpu().numpy())
+    srv.remove_scene(1)
+    with pytest.raises(IndexError):
+        srv.submit(1, reqs[0].c2w, reqs[0].cam)
+    assert srv.add_scene(str(paths[1])) == 1  # the freed slot is reused
+    tight = serve.RenderServer([], dev(), budget_bytes=1000)
+    with pytest.raises(MemoryError):
+        tight.add_scene(str(paths[0]))
