@@ -134,6 +134,11 @@ SIGNATURES = {
     "gsx_densify_count_visible": (c_int, [c_int64, P, P, P]),
     "gsx_densify_accumulate": (c_int, [c_int64, P, c_int32, P, P, c_int32, P]),
     "gsx_densify_classify": (c_int, [c_int64, P, P, P, c_float, c_float, c_int32, P, P]),
+    "gsx_adam_group_size": (c_size_t, []),
+    "gsx_photometric_loss_workspace_bytes": (c_size_t, [c_int32, c_int32]),
+    "gsx_photometric_loss_blocks": (c_int64, [c_int32, c_int32]),
+    "gsx_photometric_loss": (c_int, [P, P, c_int32, c_int32, c_int32, c_float, c_int32, P, P, P, c_size_t, P]),
+    "gsx_adam_step": (c_int, [P, P, c_int32, c_int64, P]),
     "gsx_densify_rewrite": (c_int, [c_int64, P, P, P, P, c_int64, c_int64, c_int64, P, P, P, P, c_int32, P,
                                     c_float, ctypes.c_uint64, P, P, P, P, P, P]),
 }

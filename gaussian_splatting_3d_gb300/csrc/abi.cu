@@ -447,4 +447,43 @@ int gsx_densify_rewrite(int64_t n, const uint8_t *cls, const int64_t *pos_stay,
                         out_qvec, out_log_scale, out_sh, out_alpha_logit, as_stream(stream));
 }
 
+
+// ---------------------------------------------------------------- training
+size_t gsx_adam_group_size(void) { return sizeof(gsx_adam_group); }
+
+size_t gsx_photometric_loss_workspace_bytes(int32_t height, int32_t width) {
+  if (height <= 0 || width <= 0) return 0;
+  return loss_workspace_bytes(height, width);
+}
+
+int64_t gsx_photometric_loss_blocks(int32_t height, int32_t width) {
+  if (height <= 0 || width <= 0) return 0;
+  return (3 * (int64_t)height * width + 255) / 256;
+}
+
+int gsx_photometric_loss(const float *out, const float *gt, int32_t height, int32_t width,
+                         int32_t win_size, float ssim_mult, int32_t l2, float *grad_out,
+                         float *partials, void *workspace, size_t workspace_bytes, void *stream) {
+  g_err[0] = 0;
+  GSX_REQUIRE(height > 0 && width > 0, "image size must be positive");
+  GSX_REQUIRE(win_size >= 1 && win_size <= 31 && (win_size & 1), "win_size must be odd, 1..31");
+  GSX_REQUIRE(win_size / 2 < height && win_size / 2 < width,
+              "reflected borders need the window radius below the image size");
+  GSX_REQUIRE(ssim_mult >= 0.0f && ssim_mult <= 1.0f, "ssim_mult must be in [0, 1]");
+  GSX_REQUIRE(out && gt && grad_out && workspace, "null pointer argument");
+  GSX_REQUIRE(workspace_bytes >= loss_workspace_bytes(height, width),
+              "loss workspace too small: %zu < %zu bytes", workspace_bytes,
+              loss_workspace_bytes(height, width));
+  return run_ssim_loss(out, gt, height, width, win_size, ssim_mult, l2 ? 1 : 0, grad_out, partials,
+                       workspace, as_stream(stream));
+}
+
+int gsx_adam_step(const gsx_adam_group *groups_dev, const int64_t *offsets_dev, int32_t n_groups,
+                  int64_t total, void *stream) {
+  g_err[0] = 0;
+  GSX_REQUIRE(n_groups >= 1 && total >= 0, "need at least one group and total >= 0");
+  GSX_REQUIRE(groups_dev && offsets_dev, "null pointer argument");
+  return launch_adam(groups_dev, n_groups, total, offsets_dev, as_stream(stream));
+}
+
 }  // extern "C"

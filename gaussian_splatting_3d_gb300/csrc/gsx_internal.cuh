@@ -109,6 +109,13 @@ int launch_rewrite(int64_t n, const uint8_t *cls, const int64_t *pos_stay, const
                    float *o_mean, float *o_qvec, float *o_log_scale, float *o_sh, float *o_alpha,
                    cudaStream_t s);
 
+// Training step (train.cu).
+size_t loss_workspace_bytes(int H, int W);
+int run_ssim_loss(const float *out, const float *gt, int H, int W, int win_size, float ssim_mult,
+                  int l2, float *grad_out, float *partial_out, void *ws, cudaStream_t s);
+int launch_adam(const gsx_adam_group *groups_dev, int n_groups, int64_t total,
+                const int64_t *offsets_dev, cudaStream_t s);
+
 struct RasterArgs {
   int64_t n, n_keys;  // Gaussians and list entries: bounds for start/end/ids
   int32_t width, height, tile_w, tile_h, n_tiles_w, n_tiles_h;

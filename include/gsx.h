@@ -373,6 +373,47 @@ int gsx_densify_rewrite(int64_t n, const uint8_t *cls, const int64_t *pos_stay,
                         float *out_qvec, float *out_log_scale, float *out_sh, float *out_alpha_logit,
                         void *stream);
 
+
+/*
+ * Training-step kernels (utils/loss.py:5-24, gs/sh_renderer.py:720-729).
+ *
+ * gsx_photometric_loss: for HWC float32 images out, gt [H,W,3] writes
+ * grad_out = dL/dout of L = ssim_mult * mean(clamp((1 - SSIM)/2, 0, 1)) +
+ * (1 - ssim_mult) * (l2 ? mean((out-gt)^2) : mean|out-gt|), SSIM with an
+ * odd win_size (<= 31) Gaussian window of sigma 1.5, reflected borders,
+ * C1 = 1e-4, C2 = 9e-4, eps 1e-12 (kornia's published definition).  The loss
+ * value is sum(partials[0:nb]) * ssim_mult / (3HW) + sum(partials[nb:2nb]) *
+ * (1 - ssim_mult) / (3HW), nb = gsx_photometric_loss_blocks(H, W) (partials:
+ * 2*nb floats of device memory; may be NULL).
+ *
+ * gsx_adam_step: one torch.optim.Adam step over every group of a device
+ * table: m += (1-b1)(g-m); v = b2 v + (1-b2) g^2;
+ * p -= step_size * m / (sqrt(v) / bias_correction2_sqrt + eps), where the
+ * caller sets step_size = lr / (1 - b1^t), bias_correction2_sqrt =
+ * sqrt(1 - b2^t).  offsets_dev[i] = first element of group i in the
+ * concatenation (offsets_dev[0] = 0), total = all elements.
+ */
+typedef struct gsx_adam_group {
+  float *param;
+  const float *grad;
+  float *exp_avg;
+  float *exp_avg_sq;
+  int64_t n;
+  float step_size;
+  float bias_correction2_sqrt;
+  float beta1, beta2, eps;
+  int32_t reserved;
+} gsx_adam_group;
+
+size_t gsx_adam_group_size(void);
+size_t gsx_photometric_loss_workspace_bytes(int32_t height, int32_t width);
+int64_t gsx_photometric_loss_blocks(int32_t height, int32_t width);
+int gsx_photometric_loss(const float *out, const float *gt, int32_t height, int32_t width,
+                         int32_t win_size, float ssim_mult, int32_t l2, float *grad_out,
+                         float *partials, void *workspace, size_t workspace_bytes, void *stream);
+int gsx_adam_step(const gsx_adam_group *groups_dev, const int64_t *offsets_dev, int32_t n_groups,
+                  int64_t total, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
