@@ -115,6 +115,10 @@ SIGNATURES = {
         c_int,
         [POINTER(GsxRasterParams), c_int64, c_int64, P, P, P, P, P, P, P, P, P, P, P],
     ),
+    "gsx_render_forward_maps": (
+        c_int,
+        [POINTER(GsxRasterParams), c_int64, c_int64, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P],
+    ),
     "gsx_render_backward": (
         c_int,
         [POINTER(GsxRasterParams), c_int64, c_int64, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P],

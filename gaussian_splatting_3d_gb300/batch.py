@@ -103,6 +103,8 @@ class BatchPipeline:
     def plan(self, scenes: list[Scene], views: list[ViewSpec], backward: bool = True, sh_order: int | None = None):
         dev = self.device
         st = self.settings
+        if st.bg is not None or st.output_maps:
+            raise NotImplementedError("batched passes composite no background and write no maps")
         self.scenes = scenes
         self.views = views
         self.backward_enabled = backward

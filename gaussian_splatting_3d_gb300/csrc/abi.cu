@@ -304,11 +304,12 @@ int gsx_project_forward(int64_t n, const float *mean, const float *qvec,
                                 cov2d, depth, alpha, rect, counts, as_stream(stream));
 }
 
-int gsx_render_forward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
-                       const float *mean2d, const float *cov2d, const float *sh,
-                       const float *alpha, const int32_t *start, const int32_t *end,
-                       const int32_t *gaussian_ids, const float *topleft,
-                       const float *c2w, float *out, void *stream) {
+int gsx_render_forward_maps(const gsx_raster_params *p, int64_t n, int64_t n_keys,
+                            const float *mean2d, const float *cov2d, const float *sh,
+                            const float *alpha, const int32_t *start, const int32_t *end,
+                            const int32_t *gaussian_ids, const float *topleft, const float *c2w,
+                            float *out, const float *bg_rgb, const float *depth,
+                            float *alpha_out, float *depth_out, void *stream) {
   g_err[0] = 0;
   GSX_REQUIRE(p, "null params");
   RasterArgs a = make_args(p->tile_w, p->tile_h, (uint32_t)p->n_tiles_w,
@@ -328,9 +329,28 @@ int gsx_render_forward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
   a.write_empty = p->write_empty_tiles;
   a.n = n;
   a.n_keys = n_keys;
+  if (bg_rgb) {
+    a.has_bg = 1;
+    a.bg[0] = bg_rgb[0];
+    a.bg[1] = bg_rgb[1];
+    a.bg[2] = bg_rgb[2];
+  }
+  GSX_REQUIRE(!depth_out || n == 0 || depth, "a depth map needs the per-Gaussian depth");
+  a.depth = depth;
+  a.alpha_out = alpha_out;
+  a.depth_out = depth_out;
   int st = check_raster(a, p->sh_order, n, n_keys);
   if (st != GSX_OK) return st;
   return launch_raster_forward(a, p->sh_order, as_stream(stream));
+}
+
+int gsx_render_forward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
+                       const float *mean2d, const float *cov2d, const float *sh,
+                       const float *alpha, const int32_t *start, const int32_t *end,
+                       const int32_t *gaussian_ids, const float *topleft,
+                       const float *c2w, float *out, void *stream) {
+  return gsx_render_forward_maps(p, n, n_keys, mean2d, cov2d, sh, alpha, start, end, gaussian_ids,
+                                 topleft, c2w, out, nullptr, nullptr, nullptr, nullptr, stream);
 }
 
 int gsx_render_backward(const gsx_raster_params *p, int64_t n, int64_t n_keys,

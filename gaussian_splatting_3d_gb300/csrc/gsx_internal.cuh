@@ -134,6 +134,12 @@ struct RasterArgs {
   const gsx_batch_view *views;
   int32_t n_views;
   int32_t vec_grads;  // g_mean2d 8-byte and g_cov2d 16-byte aligned (set by the launcher)
+  // forward extras (single view): background colour composited behind the
+  // Gaussians, per-pixel alpha (1 - final T) and depth (sum of T a G z)
+  int32_t has_bg;
+  float bg[3];
+  const float *depth;  // per-item camera depth (needed for depth_out)
+  float *alpha_out, *depth_out;
 };
 int launch_raster_forward(const RasterArgs &a, int C, cudaStream_t s);
 int launch_raster_backward(const RasterArgs &a, int C, cudaStream_t s);

@@ -251,6 +251,7 @@ struct SmemLayout {
   float *alpha;
   int *ids;
   float *inv_det;  // 1 / det(cov), backward only
+  float *zdep;     // camera depth, forward with a depth map only
   float *sh;
 };
 
@@ -267,6 +268,7 @@ __device__ __forceinline__ SmemLayout carve(float *smem, int B) {
   L.alpha = smem + 8 * B;
   L.ids = reinterpret_cast<int *>(smem + 9 * B);
   L.inv_det = smem + 10 * B;
+  L.zdep = smem + 11 * B;
   L.sh = smem + kRecordFloats * B;
   return L;
 }
@@ -308,7 +310,7 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 // Gaussians whose skip box meets the tile's pixel centres (in list order).
 // Requires nb <= blockDim.x.  Returns the number kept.  INV_DET also stores
 // 1 / det(cov) (the same operation the per-pair code would do).
-template <int C, bool INV_DET>
+template <int C, bool INV_DET, bool DEPTH = false>
 __device__ __forceinline__ int load_batch(const RasterArgs &a, const ViewCtx &ctx,
                                           const SmemLayout &L, int first, int nb, int t, int nthr,
                                           float tx0, float tx1, float ty0, float ty1,
@@ -352,6 +354,9 @@ __device__ __forceinline__ int load_batch(const RasterArgs &a, const ViewCtx &ct
     L.alpha[pos] = al;
     L.box[pos] = box;
     if constexpr (INV_DET) L.inv_det[pos] = 1.0f / fmaf(cv.x, cv.w, -(cv.y * cv.z));
+    if constexpr (DEPTH) {
+      if (a.depth_out) L.zdep[pos] = a.depth[id];
+    }
   }
   __syncthreads();
   const int count = total * 3 * CC;
@@ -410,7 +415,8 @@ __device__ __forceinline__ void pack_basis(const float *Y, float2 *Y2) {
     Y2[j] = make_float2(Y[2 * j], 2 * j + 1 < CC ? Y[(2 * j + 1) < CC ? 2 * j + 1 : 0] : 0.0f);
 }
 
-template <int C, int MAXT, bool BATCHED>
+// EXTRAS: background colour and alpha / depth maps (single view only).
+template <int C, int MAXT, bool BATCHED, bool EXTRAS>
 __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a) {
   constexpr int GSH = Sh<C>::GSH, CCP = Sh<C>::CCP;
   extern __shared__ float4 smem4[];
@@ -429,10 +435,16 @@ __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a
   const int n = tile_list_length(a, ctx.gtile, s0);
   if (n <= 0) {
     if (ctx.write_empty && inside) {
-      float *dst = ctx.out + 3 * ((int64_t)gy * ctx.width + gx);
-      dst[0] = 0.0f;
-      dst[1] = 0.0f;
-      dst[2] = 0.0f;
+      const int64_t pix = (int64_t)gy * ctx.width + gx;
+      float *dst = ctx.out + 3 * pix;
+      const bool bg = EXTRAS && a.has_bg;
+      dst[0] = bg ? a.bg[0] : 0.0f;
+      dst[1] = bg ? a.bg[1] : 0.0f;
+      dst[2] = bg ? a.bg[2] : 0.0f;
+      if constexpr (EXTRAS) {
+        if (a.alpha_out) a.alpha_out[pix] = 0.0f;
+        if (a.depth_out) a.depth_out[pix] = 0.0f;
+      }
     }
     return;
   }
@@ -444,7 +456,8 @@ __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a
     sh_basis<C>(ctx.c2w, px, py, Y);
     pack_basis<C>(Y, Y2);
   }
-  float o0 = 0.0f, o1 = 0.0f, o2 = 0.0f, T = 1.0f;
+  float o0 = 0.0f, o1 = 0.0f, o2 = 0.0f, T = 1.0f, dsum = 0.0f;
+  const bool want_depth = EXTRAS && a.depth_out != nullptr;
   const float thr = a.T_thresh;
   bool done = !inside;
   float tx0, tx1, ty0, ty1;
@@ -455,7 +468,7 @@ __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a
     if (__syncthreads_and(done)) break;
     const int nb = min(B, n - base);
     const int nk =
-        load_batch<C, false>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1, s_wcount);
+        load_batch<C, false, EXTRAS>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1, s_wcount);
     const int nw = __all_sync(kFull, done) ? 0 : warp_list(L, nk, blk, wl, lane);
     if (!done) {
       for (int j = 0; j < nw; ++j) {
@@ -489,16 +502,29 @@ __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a
         o0 = fmaf(coeff, y0, o0);
         o1 = fmaf(coeff, y1, o1);
         o2 = fmaf(coeff, y2, o2);
+        if constexpr (EXTRAS) {
+          if (want_depth) dsum = fmaf(coeff, L.zdep[i], dsum);
+        }
         T = T * fmaf(-al, G, 1.0f);
       }
       if (T < thr) done = true;
     }
   }
   if (inside) {
-    float *dst = ctx.out + 3 * ((int64_t)gy * ctx.width + gx);
+    const int64_t pix = (int64_t)gy * ctx.width + gx;
+    if (EXTRAS && a.has_bg) {  // what the Gaussians leave of the ray sees the background
+      o0 = fmaf(T, a.bg[0], o0);
+      o1 = fmaf(T, a.bg[1], o1);
+      o2 = fmaf(T, a.bg[2], o2);
+    }
+    float *dst = ctx.out + 3 * pix;
     dst[0] = o0;
     dst[1] = o1;
     dst[2] = o2;
+    if constexpr (EXTRAS) {
+      if (a.alpha_out) a.alpha_out[pix] = 1.0f - T;
+      if (want_depth) a.depth_out[pix] = dsum;
+    }
   }
 }
 
@@ -841,23 +867,28 @@ cudaError_t ensure_smem(K kernel, size_t smem, size_t &done) {
   return e;
 }
 
-template <int C, int MAXT, bool BATCHED>
+template <int C, int MAXT, bool BATCHED, bool EXTRAS>
 int launch_fwd_tt(RasterArgs a, int64_t grid, cudaStream_t s) {
   const int nthr = block_threads(a);
   a.batch = nthr < 128 ? nthr : 128;
   const size_t smem = fwd_smem<C>(a.batch, nthr);
   static size_t attr_done = 0;
-  cudaError_t e = ensure_smem(raster_forward_kernel<C, MAXT, BATCHED>, smem, attr_done);
+  cudaError_t e = ensure_smem(raster_forward_kernel<C, MAXT, BATCHED, EXTRAS>, smem, attr_done);
   if (e != cudaSuccess) return cuda_status(e, "raster_forward smem attribute");
   count_launches(1);
-  raster_forward_kernel<C, MAXT, BATCHED><<<(unsigned)grid, nthr, smem, s>>>(a);
+  raster_forward_kernel<C, MAXT, BATCHED, EXTRAS><<<(unsigned)grid, nthr, smem, s>>>(a);
   return cuda_status(cudaGetLastError(), "raster_forward_kernel launch");
 }
 
 template <int C, bool BATCHED>
 int launch_fwd_t(const RasterArgs &a, int64_t grid, cudaStream_t s) {
-  return block_threads(a) <= 256 ? launch_fwd_tt<C, 256, BATCHED>(a, grid, s)
-                                 : launch_fwd_tt<C, 1024, BATCHED>(a, grid, s);
+  if constexpr (!BATCHED) {
+    if (a.has_bg || a.alpha_out || a.depth_out)
+      return block_threads(a) <= 256 ? launch_fwd_tt<C, 256, false, true>(a, grid, s)
+                                     : launch_fwd_tt<C, 1024, false, true>(a, grid, s);
+  }
+  return block_threads(a) <= 256 ? launch_fwd_tt<C, 256, BATCHED, false>(a, grid, s)
+                                 : launch_fwd_tt<C, 1024, BATCHED, false>(a, grid, s);
 }
 
 template <int C, int MAXT, bool BATCHED>

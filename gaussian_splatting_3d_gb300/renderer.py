@@ -78,6 +78,10 @@ class RasterSettings:
     # projection is re-run in backward, bit-identically; the binning workspace
     # is released after each forward)
     recompute_projection: bool = False
+    # background colour composited behind the Gaussians (None: black, as the
+    # reference's default bg=False) and per-pixel alpha / depth maps
+    bg: tuple | None = None
+    output_maps: bool = False
 
     def grad_flags(self) -> int:
         if self.exact_grad:
@@ -249,9 +253,20 @@ class ViewPipeline:
             with ev("binning"):
                 ids, start, end = bin_gaussians_async(pr, ntw, nth, cap)
             with ev("raster_fwd"):
-                _lib.call("gsx_render_forward", ctypes.byref(params), n, cap, ptr(pr.mean2d), ptr(pr.cov2d),
-                          ptr(sh), ptr(pr.alpha), ptr(start), ptr(end), ptr(ids), ptr(topleft), ptr(c2w_dev),
-                          ptr(out), stream_handle(dev))
+                if settings.bg is None and not settings.output_maps:
+                    _lib.call("gsx_render_forward", ctypes.byref(params), n, cap, ptr(pr.mean2d), ptr(pr.cov2d),
+                              ptr(sh), ptr(pr.alpha), ptr(start), ptr(end), ptr(ids), ptr(topleft), ptr(c2w_dev),
+                              ptr(out), stream_handle(dev))
+                else:
+                    bg = (ctypes.c_float * 3)(*settings.bg) if settings.bg is not None else None
+                    if settings.output_maps:
+                        maps = (torch.empty((cam.h, cam.w), dtype=torch.float32, device=dev),
+                                torch.empty((cam.h, cam.w), dtype=torch.float32, device=dev))
+                    _lib.call("gsx_render_forward_maps", ctypes.byref(params), n, cap, ptr(pr.mean2d),
+                              ptr(pr.cov2d), ptr(sh), ptr(pr.alpha), ptr(start), ptr(end), ptr(ids), ptr(topleft),
+                              ptr(c2w_dev), ptr(out), ctypes.addressof(bg) if bg is not None else None,
+                              ptr(pr.depth), ptr(maps[0]) if settings.output_maps else None,
+                              ptr(maps[1]) if settings.output_maps else None, stream_handle(dev))
             st, K = binning_status(dev, n, cap, ntw, nth)
             if st == _lib.GSX_ERR_CAPACITY:
                 cap = int(K * 1.25) + 4096
@@ -269,9 +284,12 @@ class ViewPipeline:
             visible_counts = pr.counts.clone()
             pr = None
             _bin_buffers(dev).release()
-        return dict(pr=pr, ids=ids, start=start, end=end, K=K, cap=cap, topleft=topleft, c2w_dev=c2w_dev,
-                    out=out, params=params, gcam=gcam, grad_flags=settings.grad_flags(), settings=settings,
-                    counts=visible_counts)
+        st = dict(pr=pr, ids=ids, start=start, end=end, K=K, cap=cap, topleft=topleft, c2w_dev=c2w_dev,
+                  out=out, params=params, gcam=gcam, grad_flags=settings.grad_flags(), settings=settings,
+                  counts=visible_counts)
+        if settings.output_maps:
+            st["alpha_map"], st["depth_map"] = maps
+        return st
 
     def backward(self, state, mean, qvec, log_scale, sh, alpha_logit, grad_out, timer=None):
         dev = mean.device
@@ -365,8 +383,10 @@ class FusedRender(torch.autograd.Function):
         ctx.state = state
         ctx.pipe = pipe
         ctx.aux = aux
-        if aux is not None:  # per-Gaussian key counts of this view (0 = culled)
+        if aux is not None:  # per-Gaussian key counts of this view (0 = culled), optional maps
             aux["counts"] = state["counts"]
+            if "alpha_map" in state:
+                aux["alpha_map"], aux["depth_map"] = state["alpha_map"], state["depth_map"]
         return state["out"]
 
     @staticmethod
@@ -386,7 +406,11 @@ def rasterize(mean, qvec, log_scale, sh_coeffs, alpha_logit, c2w, cam: CameraInf
     tensor).  Returns the [H,W,3] image; differentiable w.r.t. all five
     parameter tensors.  With an ``aux`` dict, the forward stores the
     per-Gaussian key counts (``aux["counts"]``, 0 = culled) and the backward
-    dL/dmean2d (``aux["mean2d_grad"]``, [N,2]) for adaptive density control."""
+    dL/dmean2d (``aux["mean2d_grad"]``, [N,2]) for adaptive density control;
+    with ``settings.output_maps`` also the alpha (1 - final transmittance) and
+    depth (sum of T a G z) maps (``aux["alpha_map"]``, ``aux["depth_map"]``,
+    [H,W], not differentiated).  ``settings.bg`` composites a background
+    colour behind the Gaussians (the gradients include it)."""
     settings = settings or RasterSettings()
     if isinstance(c2w, torch.Tensor):
         c2w = c2w.detach().to("cpu", torch.float32).numpy()

@@ -43,7 +43,9 @@ class SHRenderer(torch.nn.Module):
             tile_culling_radius=float(get("tile_culling_radius", 6.0)),
             T_thresh=float(get("T_thresh", 0.01)),
             depth_detach=bool(get("depth_detach", True)),
-            exact_grad=bool(get("exact_grad", False)))
+            exact_grad=bool(get("exact_grad", False)),
+            # gs/sh_renderer.py:146-149: bg / bg_rgb (default white when enabled)
+            bg=tuple(float(v) for v in get("bg_rgb", [1.0, 1.0, 1.0])) if get("bg", False) else None)
         # adaptive density control (conf/garden_sh.yaml keys, gs/sh_renderer.py:104-151)
         self.warm_up = int(get("warm_up", 1000))
         self.adaptive_control_iteration = int(get("adaptive_control_iteration", 800))

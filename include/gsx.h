@@ -305,6 +305,23 @@ int gsx_render_forward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
                        const int32_t *gaussian_ids, const float *topleft,
                        const float *c2w, float *out, void *stream);
 
+/*
+ * gsx_render_forward with a background and output maps (no reference
+ * counterpart: the reference's background variant, vol_render_bg.h, does not
+ * compile).  bg_rgb (host pointer to 3 floats, or NULL): out += T_final * bg,
+ * where T_final is the transmittance left when the pixel stops; passing that
+ * image to gsx_render_backward makes the gradients exact for it.
+ * alpha_out f32[H*W] (or NULL) = 1 - T_final; depth_out f32[H*W] (or NULL) =
+ * sum over the composited Gaussians of T a G z with z = depth[i] (the
+ * projection's camera depth, f32[n]).  Empty tiles give bg, 0, 0.
+ */
+int gsx_render_forward_maps(const gsx_raster_params *params, int64_t n, int64_t n_keys,
+                            const float *mean2d, const float *cov2d, const float *sh,
+                            const float *alpha, const int32_t *start, const int32_t *end,
+                            const int32_t *gaussian_ids, const float *topleft, const float *c2w,
+                            float *out, const float *bg_rgb, const float *depth,
+                            float *alpha_out, float *depth_out, void *stream);
+
 /* Backward raster; grad_* are added into (caller zeroes them). */
 int gsx_render_backward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
                         const float *mean2d, const float *cov2d, const float *sh,

@@ -172,9 +172,11 @@ def tile_pixels(cam: Cam64, st: Settings64, tx: int, ty: int, device):
     return GX, GY, px, py
 
 
-def composite(px, py, Y, mean2d, cov, opac, sh, member, T_thresh):
-    """Pixels [P] x depth-ordered Gaussians [..., M] -> colours [..., P, 3].
-    member [..., M] masks Gaussians that are not on this tile's list."""
+def composite(px, py, Y, mean2d, cov, opac, sh, member, T_thresh, extras: bool = False, z=None):
+    """Pixels [P] x depth-ordered Gaussians [..., M] -> colours [..., P, 3]
+    (with extras: also the final transmittance [..., P] and the depth sum
+    sum T a G z [..., P]).  member [..., M] masks Gaussians that are not on
+    this tile's list."""
     dx = px.unsqueeze(-1) - mean2d[..., None, :, 0]
     dy = py.unsqueeze(-1) - mean2d[..., None, :, 1]
     c0, c1, c2, c3 = (cov[..., None, :, k] for k in range(4))
@@ -192,14 +194,24 @@ def composite(px, py, Y, mean2d, cov, opac, sh, member, T_thresh):
     inc = valid & (T >= T_thresh)
     wgt = torch.where(inc, T * eff, torch.zeros_like(eff))             # [..., P, M]
     col = torch.sigmoid(torch.einsum("...mck,pk->...pmc", sh, Y))      # [..., P, M, 3]
-    return (wgt.unsqueeze(-1) * col).sum(-2)
+    rgb = (wgt.unsqueeze(-1) * col).sum(-2)
+    if not extras:
+        return rgb
+    T_final = torch.where(inc, 1.0 - eff, torch.ones_like(eff)).prod(-1)
+    dsum = (wgt * z[..., None, :]).sum(-1) if z is not None else None
+    return rgb, T_final, dsum
 
 
-def render(mean, qvec, log_scale, sh, alpha_logit, cam: Cam64, st: Settings64, C: int, mode: str = "exact"):
-    """Full image [H, W, 3] (float64, differentiable)."""
+def render(mean, qvec, log_scale, sh, alpha_logit, cam: Cam64, st: Settings64, C: int, mode: str = "exact",
+           bg=None, maps: bool = False):
+    """Full image [H, W, 3] (float64, differentiable); bg: background RGB
+    composited behind (out += T_final bg); maps: also return the alpha map
+    (1 - T_final) and the depth map (sum T a G z), [H, W] each."""
     dev = mean.device
     pr = project(mean, qvec, log_scale, alpha_logit, cam, st, mode)
     img = torch.zeros((cam.h, cam.w, 3), dtype=F64, device=dev)
+    Tmap = torch.ones((cam.h, cam.w), dtype=F64, device=dev)
+    dmap = torch.zeros((cam.h, cam.w), dtype=F64, device=dev)
     ntw = (cam.w + st.tile_w - 1) // st.tile_w
     nth = (cam.h + st.tile_h - 1) // st.tile_h
     rect, keep = pr["rect"], pr["keep"]
@@ -213,16 +225,21 @@ def render(mean, qvec, log_scale, sh, alpha_logit, cam: Cam64, st: Settings64, C
             idx = idx[torch.argsort(pr["depth"].detach()[idx], stable=True)]
             GX, GY, px, py = tile_pixels(cam, st, tx, ty, dev)
             Y = sh_basis(cam, px, py, C)
-            c = composite(px, py, Y, pr["mean2d"][idx], pr["cov"][idx], pr["opac"][idx], shc[idx],
-                          torch.ones(idx.numel(), dtype=torch.bool, device=dev), st.T_thresh)
+            c, Tf, ds = composite(px, py, Y, pr["mean2d"][idx], pr["cov"][idx], pr["opac"][idx], shc[idx],
+                                  torch.ones(idx.numel(), dtype=torch.bool, device=dev), st.T_thresh,
+                                  extras=True, z=pr["depth"][idx])
             img = img.index_put((GY, GX), c)
-    return img
+            Tmap = Tmap.index_put((GY, GX), Tf)
+            dmap = dmap.index_put((GY, GX), ds)
+    if bg is not None:
+        img = img + Tmap[..., None] * torch.as_tensor(bg, dtype=F64, device=dev)
+    return (img, 1.0 - Tmap, dmap) if maps else img
 
 
-def param_grads(params64, W, cam: Cam64, st: Settings64, C: int, mode: str):
+def param_grads(params64, W, cam: Cam64, st: Settings64, C: int, mode: str, bg=None):
     """Autograd gradients of sum(W * image) in float64: dict of 5 tensors."""
     ps = [p.detach().clone().requires_grad_(True) for p in params64]
-    img = render(*ps, cam, st, C, mode)
+    img = render(*ps, cam, st, C, mode, bg=bg)
     (img * W).sum().backward()
     return dict(zip(["mean", "qvec", "log_scale", "sh", "alpha_logit"], [p.grad for p in ps])), img.detach()
 

@@ -359,17 +359,21 @@ static inline float sh_dot(const float *sh, const float *Y, int CC) {
   return s;
 }
 
-void orc_render_fwd(const orc_raster_params *P, const float *mean, const float *cov,
-                    const float *sh, const float *alpha, const int32_t *start,
-                    const int32_t *end, const int32_t *ids, const float *topleft,
-                    const float *c2w, float psx, float psy, float *out) {
+/* The forward with an optional background (out += T_final * bg), alpha map
+ * (1 - T_final) and depth map (sum of T a G z): no reference counterpart
+ * (its background variant, vol_render_bg.h, does not compile). */
+void orc_render_fwd_ex(const orc_raster_params *P, const float *mean, const float *cov,
+                       const float *sh, const float *alpha, const int32_t *start,
+                       const int32_t *end, const int32_t *ids, const float *topleft,
+                       const float *c2w, float psx, float psy, float *out, const float *bg,
+                       const float *depth, float *alpha_out, float *depth_out) {
   const int C = P->C, CC = C * C, S = P->sh_stride;
   const int64_t T = (int64_t)P->n_tiles_w * P->n_tiles_h;
 #pragma omp parallel for schedule(dynamic, 1)
   for (int64_t t = 0; t < T; ++t) {
-    if (start[t] == -1) continue;
-    int n = end[t] - start[t];
-    if (n == 0) continue;
+    const int empty = start[t] == -1 || end[t] - start[t] == 0;
+    if (empty && !bg && !alpha_out && !depth_out) continue;
+    int n = empty ? 0 : end[t] - start[t];
     int bx = (int)(t % P->n_tiles_w), by = (int)(t / P->n_tiles_w);
     for (int ly = 0; ly < P->tile_h; ++ly)
       for (int lx = 0; lx < P->tile_w; ++lx) {
@@ -378,7 +382,7 @@ void orc_render_fwd(const orc_raster_params *P, const float *mean, const float *
         float px, py, Y[16];
         pixel_pos(topleft, psx, psy, gx, gy, &px, &py);
         sh_basis(c2w, px, py, C, Y);
-        float o[3] = {0.0f, 0.0f, 0.0f}, Tr = 1.0f;
+        float o[3] = {0.0f, 0.0f, 0.0f}, Tr = 1.0f, dsum = 0.0f;
         for (int i = 0; i < n; ++i) {
           if (Tr < P->T_thresh) break;
           int g = ids[start[t] + i];
@@ -393,12 +397,26 @@ void orc_render_fwd(const orc_raster_params *P, const float *mean, const float *
             if (isnan(y * coeff)) y = 0.0f;
             o[ch] = fmaf(coeff, y, o[ch]);
           }
+          if (depth_out) dsum = fmaf(coeff, depth[g], dsum);
           Tr = Tr * fmaf(-a, G, 1.0f);
         }
-        float *dst = out + 3 * ((int64_t)gy * P->width + gx);
+        const int64_t pix = (int64_t)gy * P->width + gx;
+        if (bg)
+          for (int ch = 0; ch < 3; ++ch) o[ch] = fmaf(Tr, bg[ch], o[ch]);
+        float *dst = out + 3 * pix;
         dst[0] = o[0]; dst[1] = o[1]; dst[2] = o[2];
+        if (alpha_out) alpha_out[pix] = 1.0f - Tr;
+        if (depth_out) depth_out[pix] = dsum;
       }
   }
+}
+
+void orc_render_fwd(const orc_raster_params *P, const float *mean, const float *cov,
+                    const float *sh, const float *alpha, const int32_t *start,
+                    const int32_t *end, const int32_t *ids, const float *topleft,
+                    const float *c2w, float psx, float psy, float *out) {
+  orc_render_fwd_ex(P, mean, cov, sh, alpha, start, end, ids, topleft, c2w, psx, psy, out, NULL,
+                    NULL, NULL, NULL);
 }
 
 static inline void atomic_addf(float *p, float v) {

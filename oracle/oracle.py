@@ -168,12 +168,20 @@ def raster_params(width, height, tile_w, tile_h, C, sh_stride=None, T_thresh=0.0
     return p
 
 
-def render_fwd(P: OrcRasterParams, mean2d, cov2d, sh, alpha, start, end, ids, topleft, c2w, psx, psy):
+def render_fwd(P: OrcRasterParams, mean2d, cov2d, sh, alpha, start, end, ids, topleft, c2w, psx, psy,
+               bg=None, depth=None, maps: bool = False):
+    """Image [H,W,3]; with maps=True also (alpha map, depth map) [H,W] (depth
+    needs the per-Gaussian depth).  bg: background RGB composited behind."""
     out = np.zeros((P.height, P.width, 3), np.float32)
-    lib().orc_render_fwd(ctypes.byref(P), _p(f32(mean2d)), _p(f32(cov2d)), _p(f32(sh)), _p(f32(alpha)),
-                         _p(i32(start)), _p(i32(end)), _p(i32(ids)), _p(f32(topleft)), _p(f32(c2w)),
-                         c_float(psx), c_float(psy), _p(out))
-    return out
+    am = np.zeros((P.height, P.width), np.float32) if maps else None
+    dm = np.zeros((P.height, P.width), np.float32) if maps and depth is not None else None
+    bgv = f32(np.asarray(bg, np.float32)) if bg is not None else None
+    lib().orc_render_fwd_ex(ctypes.byref(P), _p(f32(mean2d)), _p(f32(cov2d)), _p(f32(sh)), _p(f32(alpha)),
+                            _p(i32(start)), _p(i32(end)), _p(i32(ids)), _p(f32(topleft)), _p(f32(c2w)),
+                            c_float(psx), c_float(psy), _p(out), _p(bgv) if bgv is not None else None,
+                            _p(f32(depth)) if dm is not None else None, _p(am) if am is not None else None,
+                            _p(dm) if dm is not None else None)
+    return (out, am, dm) if maps else out
 
 
 def render_bwd(P: OrcRasterParams, mean2d, cov2d, sh, alpha, start, end, ids, topleft, c2w, psx, psy, out,
@@ -211,7 +219,7 @@ def num_threads() -> int:
 
 
 def render_view(scene, view, grad_weight=None, frustum_radius=1.0, tile_radius=6.0, T_thresh=0.01,
-                sh_order=None, grad_flags: int = 0):
+                sh_order=None, grad_flags: int = 0, bg=None):
     """Full oracle pipeline for one view of a scene.Scene / scene.View:
     project, bin, raster forward and (if grad_weight is given) backward
     through the projection.  Returns a dict of every intermediate."""
@@ -229,9 +237,9 @@ def render_view(scene, view, grad_weight=None, frustum_radius=1.0, tile_radius=6
     P = raster_params(cam.w, cam.h, view.tile, view.tile, C, scene.sh.shape[-1], T_thresh)
     topleft = np.array(cam.topleft(), np.float32)
     psx, psy = np.float32(1.0 / cam.fx), np.float32(1.0 / cam.fy)
-    img = render_fwd(P, pr["mean2d"], pr["cov2d"], scene.sh, pr["alpha"], b["start"], b["end"], b["ids"],
-                     topleft, view.c2w, psx, psy)
-    res = dict(proj=pr, bins=b, image=img, camera=ocam, params=P, topleft=topleft)
+    img, am, dm = render_fwd(P, pr["mean2d"], pr["cov2d"], scene.sh, pr["alpha"], b["start"], b["end"], b["ids"],
+                             topleft, view.c2w, psx, psy, bg=bg, depth=pr["depth"], maps=True)
+    res = dict(proj=pr, bins=b, image=img, alpha_map=am, depth_map=dm, camera=ocam, params=P, topleft=topleft)
     if grad_weight is not None:
         g = render_bwd(P, pr["mean2d"], pr["cov2d"], scene.sh, pr["alpha"], b["start"], b["end"], b["ids"],
                        topleft, view.c2w, psx, psy, img, grad_weight)
