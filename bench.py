@@ -609,7 +609,7 @@ def run_reference_cuda(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)  # ~0.75 s timed: a few clock samples
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gsx", choices=["gsx", "reference", "reference-cuda"])
     ap.add_argument("--workload", default="headline", choices=["headline", "small", "batch", "serve", "memory"])
