@@ -119,6 +119,19 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(value: float, world: int, device=None) -> float:
+    """The largest `value` over the ranks (the slowest replica's step time);
+    the value itself on one rank.  Works on any process-group backend."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def algorithmic_bytes(stage, n, K, P, C, n_tiles):
     """Per-launch bytes of each stage, with the per-unit figures documented
     for the roofline: per Gaussian for the projection passes, per key and per
@@ -195,13 +208,7 @@ def run_gsx(args):
     wall1 = time.perf_counter()
     launches = int(_lib.load().gsx_kernel_launch_count() - launches0)
     clock_info = clocks.stop()
-    ms = t0.elapsed_time(t1) / args.steps
-    if world > 1:
-        import torch.distributed as dist
-
-        tt = torch.tensor([ms], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = max_over_ranks(t0.elapsed_time(t1) / args.steps, world, dev)
     stages = timer.summary()
 
     # end-to-end through the public autograd API with host buffers
@@ -233,7 +240,7 @@ def run_gsx(args):
         e2e_step()
     e1.record()
     barrier()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, dev)
     h2d = sum(h.numel() * 4 for h in host) + Wh.numel() * 4
     d2h = sum(o.numel() * 4 for o in out_host) + img_host.numel() * 4 + 4
 
@@ -606,13 +613,83 @@ def run_reference_cuda(args):
                       "the reference's CUDA backward trips its own device assert (vol_render_sh.h:448-452: "
                       "recomputed colour != stored colour) on GB300; faulting reference GPU code is not re-run"}))
 
+def run_train(args):
+    """One training iteration of the reference's loop (main_sh.py:150-240) on
+    the headline scene: render, SSIM + L2 loss (ssim_loss_mult 0.2, window 11),
+    backward, Adam step over the five parameter groups (per-group learning
+    rates of conf/garden_sh.yaml:72-76), all on this package's kernels."""
+    import torch
+
+    from gaussian_splatting_3d_gb300 import _lib, renderer, scene as S, train
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    wl = S.headline_workload(n=args.n)
+    sc, view = wl.scene, wl.views[0]
+    params = [torch.nn.Parameter(torch.from_numpy(a).to(dev)) for a in
+              (sc.mean, sc.qvec, sc.log_scale, sc.sh, sc.alpha_logit)]
+    gt = torch.from_numpy(wl.grad_weight).to(dev)  # a seeded U[0,1] target image
+    lrs = [1e-3, 1e-2, 1e-2, 1e-2, 1e-2]
+    opt = train.FusedAdam([{"params": [p], "lr": lr} for p, lr in zip(params, lrs)], betas=(0.9, 0.99))
+    lset = train.LossSettings(ssim_mult=0.2, win_size=11, loss_fn="l2")
+    st = renderer.RasterSettings()
+    ev = {k: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for k in
+          ("render", "loss", "backward", "adam")}
+    acc = {k: 0.0 for k in ev}
+
+    def step(timed=False):
+        e = ev if timed else None
+        if e: e["render"][0].record()
+        img = renderer.rasterize(*params, view.c2w, view.cam, st)
+        if e: e["render"][1].record(); e["loss"][0].record()
+        loss = train.photometric_loss(img, gt, lset)
+        if e: e["loss"][1].record(); e["backward"][0].record()
+        for p in params:
+            p.grad = None
+        loss.backward()
+        if e: e["backward"][1].record(); e["adam"][0].record()
+        opt.step()
+        if e: e["adam"][1].record()
+        return loss
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    launches0 = _lib.load().gsx_kernel_launch_count()
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for _ in range(args.steps):
+        loss = step(timed=True)
+        torch.cuda.synchronize()
+        for k, (a, b) in ev.items():
+            acc[k] += a.elapsed_time(b)
+    t1.record()
+    torch.cuda.synchronize()
+    clock_info = clocks.stop()
+    ms = t0.elapsed_time(t1) / args.steps
+    line = {
+        "metric": "training iteration ms/iter (render + SSIM/L2 loss + backward + Adam; 1M Gaussians, 1920x1080)",
+        "value": round(ms, 4), "unit": "ms/iter", "higher_is_better": False, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene and target image; no dataset)",
+        "stages_ms": {k: round(v / args.steps, 4) for k, v in acc.items()},
+        "loss": float(loss), "gpu_launches": int(_lib.load().gsx_kernel_launch_count() - launches0),
+        "clocks": clock_info,
+        "config": {"workload": "train: headline scene, loss ssim_mult 0.2 window 11 l2, Adam betas (0.9, 0.99)",
+                   "note": "synchronised after each step to read the stage events"},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)  # ~0.75 s timed: a few clock samples
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gsx", choices=["gsx", "reference", "reference-cuda"])
-    ap.add_argument("--workload", default="headline", choices=["headline", "small", "batch", "serve", "memory"])
+    ap.add_argument("--workload", default="headline", choices=["headline", "small", "batch", "serve", "memory", "train"])
     ap.add_argument("--views", type=int, default=32)
     ap.add_argument("--n-batch", type=int, default=500_000)
     ap.add_argument("--n", type=int, default=1_000_000)
@@ -639,6 +716,8 @@ def main():
         run_serve(args)
     elif args.workload == "memory":
         run_memory(args)
+    elif args.workload == "train":
+        run_train(args)
     else:
         run_gsx(args)
 
