@@ -392,6 +392,12 @@ int gsx_render_backward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
   return launch_raster_backward(a, p->sh_order, as_stream(stream));
 }
 
+int gsx_raster_status(uint32_t *flags, int32_t clear, void *stream) {
+  g_err[0] = 0;
+  GSX_REQUIRE(flags, "null flags pointer");
+  return raster_status(flags, clear, as_stream(stream));
+}
+
 int gsx_project_backward(int64_t n, const float *mean, const float *qvec,
                          const float *log_scale, const float *alpha_logit,
                          const gsx_camera *cam, const int32_t *counts,

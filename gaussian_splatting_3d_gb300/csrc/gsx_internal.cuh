@@ -147,6 +147,9 @@ int launch_raster_backward(const RasterArgs &a, int C, cudaStream_t s);
 // shape and SH order; the per-view fields of `a` are ignored).
 int launch_raster_forward_batch(const RasterArgs &a, int C, int64_t total_tiles, cudaStream_t s);
 int launch_raster_backward_batch(const RasterArgs &a, int C, int64_t total_tiles, cudaStream_t s);
+// Sticky error bits of the raster kernels (synchronises `s`); clear != 0
+// resets them.
+int raster_status(uint32_t *flags, int clear, cudaStream_t s);
 
 // Binning.  rect_tl/rect_br point at int32 pairs with `rect_stride` ints per
 // Gaussian (4 for packed [n,4] rects, 2 for separate [n,2] arrays).

@@ -40,9 +40,16 @@
 
 namespace gsx {
 
+// Sticky error bits of the raster kernels (read and cleared by
+// raster_status); kRasterErrTimeout: a bulk-copy barrier wait gave up.
+__device__ uint32_t g_raster_flags = 0;
+
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
+// polls of a bulk-copy barrier before the raster gives up and flags the error
+constexpr uint32_t kBulkWaitLimit = 1u << 20;
+constexpr uint32_t kRasterErrTimeout = 1u;  // bit of g_raster_flags
 
 template <int C>
 struct Sh {
@@ -306,17 +313,81 @@ __device__ __forceinline__ unsigned lanemask_lt() {
   return lt;
 }
 
+// ---- bulk-copy (TMA engine) staging of the SH rows -------------------------
+// A batch's SH rows are copied global -> shared with cp.async.bulk, one copy
+// per kept Gaussian (or per channel when the rows are strided), completing on
+// one mbarrier per CTA.  Thread 0 arms the barrier with the batch's byte
+// total; the phase flips once per batch.
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for the phase `parity` of `bar`; false if it did not complete.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kBulkWaitLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes,
+                                              uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// The SH rows of this CTA's scene can be bulk-copied: every copy starts on a
+// 16-byte boundary and moves a multiple of 16 bytes (C*C and the row stride
+// multiples of 4 floats, base 16-byte aligned).
+template <int C>
+__device__ __forceinline__ bool sh_bulk_ok(const float *sh, int sh_stride) {
+  return (C * C) % 4 == 0 && (sh_stride & 3) == 0 &&
+         (reinterpret_cast<uintptr_t>(sh) & 15) == 0;
+}
+
 // Gather one batch of the tile's list into shared memory, keeping only the
 // Gaussians whose skip box meets the tile's pixel centres (in list order).
-// Requires nb <= blockDim.x.  Returns the number kept.  INV_DET also stores
-// 1 / det(cov) (the same operation the per-pair code would do).
+// Requires nb <= blockDim.x.  Returns the number kept, or -1 (for the whole
+// CTA) if a bulk-copy wait gave up.  INV_DET also stores 1 / det(cov) (the
+// same operation the per-pair code would do).  When the SH rows allow it
+// (sh_bulk_ok), each kept Gaussian's rows arrive by cp.async.bulk on `bar`
+// (phase `parity`, initialised by the kernel); otherwise the CTA copies them
+// with ordinary loads.
 template <int C, bool INV_DET, bool DEPTH = false>
 __device__ __forceinline__ int load_batch(const RasterArgs &a, const ViewCtx &ctx,
                                           const SmemLayout &L, int first, int nb, int t, int nthr,
                                           float tx0, float tx1, float ty0, float ty1,
-                                          int *s_wcount) {
+                                          int *s_wcount, uint64_t *bar, uint32_t parity) {
   constexpr int CC = Sh<C>::CC, CCP = Sh<C>::CCP, GSH = Sh<C>::GSH;
   const int lane = t & 31, warp = t >> 5, nwarps = nthr >> 5;
+  const bool bulk = sh_bulk_ok<C>(ctx.sh, ctx.sh_stride);  // CTA-uniform
   bool keep = false;
   int id = -1;
   float2 mm = make_float2(0.0f, 0.0f), box = make_float2(0.0f, 0.0f);
@@ -346,6 +417,7 @@ __device__ __forceinline__ int load_batch(const RasterArgs &a, const ViewCtx &ct
     before += (w < warp) ? c : 0;
     total += c;
   }
+  if (bulk && t == 0) mbar_arrive_expect_tx(bar, (uint32_t)(total * 3 * CC * sizeof(float)));
   if (keep) {
     const int pos = before + __popc(ballot & lanemask_lt());
     L.ids[pos] = id;
@@ -357,6 +429,30 @@ __device__ __forceinline__ int load_batch(const RasterArgs &a, const ViewCtx &ct
     if constexpr (DEPTH) {
       if (a.depth_out) L.zdep[pos] = a.depth[id];
     }
+    if (bulk) {
+      // the previous batch's reads of this slot finished before the barrier
+      // above; order them before the async-proxy writes
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      const int64_t g = (int64_t)id - ctx.item_lo;
+      const float *src = ctx.sh + g * 3 * ctx.sh_stride;
+      float *dst = L.sh + pos * GSH;
+      if (ctx.sh_stride == CC) {
+        bulk_copy_g2s(dst, src, 3 * CC * sizeof(float), bar);
+      } else {
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch)
+          bulk_copy_g2s(dst + ch * CCP, src + ch * ctx.sh_stride, CC * sizeof(float), bar);
+      }
+    }
+  }
+  if (bulk) {
+    bool ok = mbar_wait_bounded(bar, parity);
+    if (!ok) {
+      atomicOr(&g_raster_flags, kRasterErrTimeout);
+      ok = mbar_wait_bounded(bar, parity);  // the copies may still land: wait once more
+    }
+    // records visible to all threads; the CTA leaves together if any wait gave up
+    return __syncthreads_or(!ok) ? -1 : total;
   }
   __syncthreads();
   const int count = total * 3 * CC;
@@ -421,6 +517,7 @@ __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a
   constexpr int GSH = Sh<C>::GSH, CCP = Sh<C>::CCP;
   extern __shared__ float4 smem4[];
   __shared__ int s_wcount[32];
+  __shared__ uint64_t s_bar;  // bulk-copy barrier of the SH rows
   const int nthr = blockDim.x;
   const int B = a.batch;
   SmemLayout L = carve<C>(reinterpret_cast<float *>(smem4), B);
@@ -463,12 +560,15 @@ __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a
   float tx0, tx1, ty0, ty1;
   tile_bounds(ctx, tx0, tx1, ty0, ty1);
   const float4 blk = warp_block(px, py);
+  if (t == 0 && sh_bulk_ok<C>(ctx.sh, ctx.sh_stride))
+    mbar_init(&s_bar);  // ordered before use by the loop's first barrier
 
   for (int base = 0; base < n; base += B) {
     if (__syncthreads_and(done)) break;
     const int nb = min(B, n - base);
-    const int nk =
-        load_batch<C, false, EXTRAS>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1, s_wcount);
+    const int nk = load_batch<C, false, EXTRAS>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0,
+                                                ty1, s_wcount, &s_bar, (uint32_t)(base / B) & 1u);
+    if (nk < 0) return;  // flagged in g_raster_flags
     const int nw = __all_sync(kFull, done) ? 0 : warp_list(L, nk, blk, wl, lane);
     if (!done) {
       for (int j = 0; j < nw; ++j) {
@@ -647,6 +747,7 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
   constexpr int NV = Grad<C>::NV, CSTR = Grad<C>::CSTR;  // gm0 gm1 gc0 gc12 gc3 galpha gsh
   extern __shared__ float4 smem4[];
   __shared__ int s_wcount[32];
+  __shared__ uint64_t s_bar;  // bulk-copy barrier of the SH rows
   float *smem = reinterpret_cast<float *>(smem4);
   const int B = a.batch;
   const int nthr = blockDim.x, nwarps = nthr >> 5;
@@ -695,14 +796,17 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
   float tx0, tx1, ty0, ty1;
   tile_bounds(ctx, tx0, tx1, ty0, ty1);
   const float4 blk = warp_block(px, py);
+  if (t == 0 && sh_bulk_ok<C>(ctx.sh, ctx.sh_stride))
+    mbar_init(&s_bar);  // ordered before use by the loop's first barrier
 
   for (int base = 0; base < n; base += B) {
     if (__syncthreads_and(done)) break;
     const int nb = min(B, n - base);
     for (int f = t; f < nb * NV; f += nthr) s_grad[f] = 0.0f;
     for (int j = t; j < nb; j += nthr) s_touched[j] = 0;
-    const int nk =
-        load_batch<C, true>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1, s_wcount);
+    const int nk = load_batch<C, true>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1,
+                                       s_wcount, &s_bar, (uint32_t)(base / B) & 1u);
+    if (nk < 0) return;  // flagged in g_raster_flags
     const int nw = __all_sync(kFull, done) ? 0 : warp_list(L, nk, blk, wl, lane);
 
     int nslot = 0;  // warp-uniform: Gaussians staged in this warp's weight matrix
@@ -960,6 +1064,19 @@ int launch_raster_forward_batch(const RasterArgs &a, int C, int64_t total_tiles,
 int launch_raster_backward_batch(const RasterArgs &a, int C, int64_t total_tiles, cudaStream_t s) {
   if (total_tiles == 0) return GSX_OK;
   return dispatch_bwd<true>(a, C, total_tiles, s);
+}
+
+int raster_status(uint32_t *flags, int clear, cudaStream_t s) {
+  cudaError_t e = cudaMemcpyFromSymbolAsync(flags, g_raster_flags, sizeof(uint32_t), 0,
+                                            cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess && clear && *flags) {
+    const uint32_t zero = 0;
+    e = cudaMemcpyToSymbolAsync(g_raster_flags, &zero, sizeof(uint32_t), 0,
+                                cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  return cuda_status(e, "raster status");
 }
 
 }  // namespace gsx

@@ -206,6 +206,17 @@ def binning_status(dev, n: int, capacity: int, n_tiles_w: int, n_tiles_h: int):
     return st, int(k.value)
 
 
+def raster_status(dev=None, clear: bool = True) -> int:
+    """Sticky error bits of the raster kernels on `dev` (synchronises; 0 =
+    no error).  Bit 0: a wait for the bulk copies of a batch's SH rows gave
+    up, so some tile's output or gradients are incomplete."""
+    dev = torch.device(dev) if dev is not None else torch.device("cuda", torch.cuda.current_device())
+    flags = ctypes.c_uint32(0)
+    with torch.cuda.device(dev):
+        _lib.call("gsx_raster_status", ctypes.addressof(flags), 1 if clear else 0, stream_handle(dev))
+    return int(flags.value)
+
+
 def _raster_params(cam: CameraInfo, settings: RasterSettings, C: int, sh_stride: int) -> GsxRasterParams:
     ntw, nth = settings.tiles(cam)
     p = GsxRasterParams()

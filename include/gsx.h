@@ -333,6 +333,15 @@ int gsx_render_backward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
                         void *stream);
 
 /*
+ * Sticky error bits of every raster launch of this process on the current
+ * device (no reference counterpart: the reference's kernels trap instead).
+ * Bit 0: a wait for the bulk copies (cp.async.bulk) that stage a batch's SH
+ * rows in shared memory gave up; that tile's output or gradients are
+ * incomplete.  Synchronises `stream`; clear != 0 resets the bits.
+ */
+int gsx_raster_status(uint32_t *flags, int32_t clear, void *stream);
+
+/*
  * Projection backward from the raster gradients grad_mean2d f32[n,2],
  * grad_cov2d f32[n,4], grad_alpha f32[n] to the parameter gradients
  * grad_mean f32[n,3], grad_qvec f32[n,4], grad_log_scale f32[n,3],

@@ -26,3 +26,15 @@ def pytest_collection_modifyitems(config, items):
     for item in items:
         if "gpu" in item.keywords:
             item.add_marker(skip)
+
+
+@pytest.fixture
+def raster_flags_clean():
+    """Fails the test if a raster kernel flagged an error (e.g. a bulk-copy
+    wait that gave up) while it ran."""
+    from gaussian_splatting_3d_gb300 import renderer
+
+    renderer.raster_status(clear=True)
+    yield
+    flags = renderer.raster_status(clear=True)
+    assert flags == 0, f"raster kernels flagged errors: 0x{flags:x}"

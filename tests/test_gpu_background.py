@@ -20,7 +20,7 @@ from gaussian_splatting_3d_gb300.sh_renderer import SHRenderer  # noqa: E402
 from oracle import fp64_render as R  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
-pytestmark = pytest.mark.gpu
+pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("raster_flags_clean")]
 BG = (0.2, 0.5, 0.9)
 KEYS = ["mean", "qvec", "log_scale", "sh", "alpha_logit"]
 

@@ -16,7 +16,7 @@ from gaussian_splatting_3d_gb300 import batch as B  # noqa: E402
 from gaussian_splatting_3d_gb300 import renderer, scene as S  # noqa: E402
 from gaussian_splatting_3d_gb300.camera import CameraInfo, look_at_c2w  # noqa: E402
 
-pytestmark = pytest.mark.gpu
+pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("raster_flags_clean")]
 GRAD_REL = 1e-4
 
 

@@ -23,7 +23,7 @@ torch = pytest.importorskip("torch")
 from gaussian_splatting_3d_gb300 import _gs, renderer  # noqa: E402
 from gaussian_splatting_3d_gb300.camera import CameraInfo  # noqa: E402
 
-pytestmark = pytest.mark.gpu
+pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("raster_flags_clean")]
 GOLDEN = sorted(p for p in (Path(__file__).parent / "golden").glob("*.npz") if not p.stem.startswith("densify"))
 IMG_TOL = 1e-4
 GRAD_REL = 1e-4

@@ -22,7 +22,7 @@ from gaussian_splatting_3d_gb300 import batch as B  # noqa: E402
 from gaussian_splatting_3d_gb300 import renderer, scene as S  # noqa: E402
 from oracle import fp64_render as R  # noqa: E402
 
-pytestmark = pytest.mark.gpu
+pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("raster_flags_clean")]
 GRAD_REL = 1e-4
 KEYS = ["mean", "qvec", "log_scale", "sh", "alpha_logit"]
 WORKLOADS = {"diff": {}, "diff_clamp": dict(log_scale_mu=-2.0, alpha_mu=3.0)}

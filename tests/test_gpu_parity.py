@@ -20,7 +20,7 @@ from gaussian_splatting_3d_gb300 import _gs, renderer, scene as S  # noqa: E402
 from gaussian_splatting_3d_gb300.camera import CameraInfo, look_at_c2w  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
-pytestmark = pytest.mark.gpu
+pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("raster_flags_clean")]
 
 GRAD_REL = 1e-4
 IMG_ATOL = 2e-6

@@ -18,7 +18,7 @@ from gaussian_splatting_3d_gb300 import batch as B  # noqa: E402
 from gaussian_splatting_3d_gb300 import renderer, scene as S, serve  # noqa: E402
 from gaussian_splatting_3d_gb300.camera import CameraInfo, look_at_c2w  # noqa: E402
 
-pytestmark = pytest.mark.gpu
+pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("raster_flags_clean")]
 
 SIZES = ((96, 80), (128, 96), (64, 64), (160, 90))
 
