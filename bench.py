@@ -8,9 +8,11 @@ all five parameter tensors.  Metric: fwd+bwd ms/iter (lower is better).
 
 Printed JSON line (rank 0): value = device-timed ms per step with the scene
 resident in HBM (CUDA events over K steps, max over ranks); ``e2e`` = the same
-step through the public API with pinned host buffers, host->device copy of the
-parameters and the loss weights and device->host copy of the image and all
-gradients inside the timed region; ``roofline`` for the dominant kernel from
+step through the public API (``rasterize`` on pinned host parameters), with
+the host->device copy of the parameters and the loss weights and the
+device->host copy of the image, the loss and all gradients inside the timed
+region (the SH upload overlaps projection and binning, the image download
+overlaps the backward); ``roofline`` for the dominant kernel from
 per-stage CUDA events inside the timed region; ``cpu_baseline`` = the CPU
 oracle on a bounded sample of the same workload.
 
@@ -211,24 +213,36 @@ def run_gsx(args):
     ms = max_over_ranks(t0.elapsed_time(t1) / args.steps, world, dev)
     stages = timer.summary()
 
-    # end-to-end through the public autograd API with host buffers
+    # end-to-end through the public autograd API with host-resident (pinned)
+    # parameters: every step uploads the parameters and the loss weights and
+    # brings back the image, the loss and all five gradients.  rasterize
+    # overlaps the SH upload with projection and binning; the image download
+    # overlaps the backward; the gradients land in the host leaves' .grad.
     host = [torch.from_numpy(a).pin_memory() for a in (sc.mean, sc.qvec, sc.log_scale, sc.sh, sc.alpha_logit)]
     Wh = torch.from_numpy(wl.grad_weight).pin_memory()
-    out_host = [torch.empty(a.shape, dtype=torch.float32).pin_memory() for a in
-                (sc.mean, sc.qvec, sc.log_scale, sc.sh, sc.alpha_logit)]
     img_host = torch.empty((view.cam.h, view.cam.w, 3), dtype=torch.float32).pin_memory()
     loss_host = torch.empty((), dtype=torch.float32).pin_memory()
+    side = torch.cuda.Stream(dev)
+    main = torch.cuda.current_stream(dev)
+    e2e_grads = []
 
     def e2e_step():
-        ps = [h.to(dev, non_blocking=True).requires_grad_(True) for h in host]
-        w = Wh.to(dev, non_blocking=True)
-        img = renderer.rasterize(*ps, view.c2w, view.cam, settings)
+        ps = [h.detach().requires_grad_(True) for h in host]
+        side.wait_stream(main)
+        with torch.cuda.stream(side):
+            w = Wh.to(dev, non_blocking=True)
+        img = renderer.rasterize(*ps, view.c2w, view.cam, settings, device=dev)
+        main.wait_stream(side)
+        w.record_stream(main)
+        side.wait_stream(main)
+        with torch.cuda.stream(side):
+            img_host.copy_(img.detach(), non_blocking=True)
+        img.record_stream(side)
         loss = (img * w).sum()
-        loss.backward()
-        for p, o in zip(ps, out_host):
-            o.copy_(p.grad, non_blocking=True)
-        img_host.copy_(img.detach(), non_blocking=True)
+        loss.backward()  # returns with the host gradients complete
         loss_host.copy_(loss.detach(), non_blocking=True)
+        main.wait_stream(side)
+        e2e_grads[:] = [p.grad for p in ps]
 
     for _ in range(max(1, args.warmup)):
         e2e_step()
@@ -241,8 +255,10 @@ def run_gsx(args):
     e1.record()
     barrier()
     e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, dev)
+    for g, h in zip(e2e_grads, host):
+        assert g is not None and not g.is_cuda and g.shape == h.shape
     h2d = sum(h.numel() * 4 for h in host) + Wh.numel() * 4
-    d2h = sum(o.numel() * 4 for o in out_host) + img_host.numel() * 4 + 4
+    d2h = sum(g.numel() * 4 for g in e2e_grads) + img_host.numel() * 4 + 4
 
     if rank != 0:
         return

@@ -10,6 +10,7 @@ coordinates: pixel (px, py) sits at ``topleft + (px, py) / (fx, fy)`` with
 from __future__ import annotations
 
 import math
+from collections import OrderedDict
 
 import numpy as np
 import torch
@@ -138,8 +139,22 @@ def frustum_np(c2w: np.ndarray, cam: CameraInfo):
     return n.numpy().astype(np.float32), p.numpy().astype(np.float32)
 
 
+_CAMERA_CACHE: "OrderedDict[tuple, GsxCamera]" = OrderedDict()
+_CAMERA_CACHE_SIZE = 256
+
+
 def make_gsx_camera(c2w: np.ndarray, cam: CameraInfo) -> GsxCamera:
+    """Camera record of the native projection (c2w, intrinsics, image size,
+    frustum half-spaces).  The frustum costs ~0.2 ms of small torch CPU ops,
+    so records are memoised on the exact camera (c2w bits and every
+    CameraInfo field); callers must not modify the returned record."""
     c2w = np.ascontiguousarray(c2w, dtype=np.float32).reshape(3, 4)
+    key = (c2w.tobytes(), float(cam.fx), float(cam.fy), float(cam.cx), float(cam.cy), int(cam.w), int(cam.h),
+           float(cam.yfov), float(cam.aspect), float(cam.near_plane), float(cam.far_plane))
+    g = _CAMERA_CACHE.get(key)
+    if g is not None:
+        _CAMERA_CACHE.move_to_end(key)
+        return g
     normals, pts = frustum_np(c2w, cam)
     g = GsxCamera()
     g.c2w[:] = [float(v) for v in c2w.reshape(-1)]
@@ -147,4 +162,7 @@ def make_gsx_camera(c2w: np.ndarray, cam: CameraInfo) -> GsxCamera:
     g.width, g.height = int(cam.w), int(cam.h)
     g.frustum_normals[:] = [float(v) for v in normals.reshape(-1)]
     g.frustum_pts[:] = [float(v) for v in pts.reshape(-1)]
+    _CAMERA_CACHE[key] = g
+    if len(_CAMERA_CACHE) > _CAMERA_CACHE_SIZE:
+        _CAMERA_CACHE.popitem(last=False)
     return g

@@ -230,6 +230,15 @@ def _raster_params(cam: CameraInfo, settings: RasterSettings, C: int, sh_stride:
     return p
 
 
+def camera_consts(c2w_np, cam: CameraInfo) -> torch.Tensor:
+    """Pinned host tensor [14]: the image-plane top-left corner (2 floats)
+    and the row-major [3,4] camera-to-world matrix the raster reads."""
+    t = torch.empty(14, dtype=torch.float32, pin_memory=True)
+    t[:2] = torch.tensor(cam.topleft(), dtype=torch.float32)
+    t[2:] = torch.from_numpy(np.ascontiguousarray(c2w_np, dtype=np.float32).reshape(12))
+    return t
+
+
 class ViewPipeline:
     """One view through the fused native path with persistent device buffers.
 
@@ -244,7 +253,11 @@ class ViewPipeline:
         self.key_capacity = 0  # grows to ~1.25x the largest key count seen
 
     def forward(self, mean, qvec, log_scale, sh, alpha_logit, c2w_np, cam: CameraInfo,
-                settings: RasterSettings, timer=None):
+                settings: RasterSettings, timer=None, sh_ready=None, cam_consts=None):
+        """``sh_ready``: an event the raster stage waits for (the SH
+        coefficients still arriving on a copy stream while projection and
+        binning run); ``cam_consts``: the device copy of
+        ``camera_consts(c2w_np, cam)`` when the caller uploaded it."""
         dev = mean.device
         n = mean.shape[0]
         sh_stride = sh.shape[-1]
@@ -254,15 +267,17 @@ class ViewPipeline:
         with ev("project"):
             pr = project(mean, qvec, log_scale, alpha_logit, gcam, settings)
         ntw, nth = settings.tiles(cam)
-        topleft = torch.tensor(cam.topleft(), dtype=torch.float32).to(dev, non_blocking=True)
-        c2w_dev = torch.from_numpy(np.ascontiguousarray(c2w_np, dtype=np.float32)).reshape(3, 4).to(
-            dev, non_blocking=True)
+        if cam_consts is None:
+            cam_consts = camera_consts(c2w_np, cam).to(dev, non_blocking=True)
+        topleft, c2w_dev = cam_consts[:2], cam_consts[2:]
         out = torch.empty((cam.h, cam.w, 3), dtype=torch.float32, device=dev)
         params = _raster_params(cam, settings, C, sh_stride)
         cap = max(self.key_capacity, 1 << 16)
         for _ in range(3):
             with ev("binning"):
                 ids, start, end = bin_gaussians_async(pr, ntw, nth, cap)
+            if sh_ready is not None:  # only the raster reads the SH coefficients
+                torch.cuda.current_stream(dev).wait_event(sh_ready)
             with ev("raster_fwd"):
                 if settings.bg is None and not settings.output_maps:
                     _lib.call("gsx_render_forward", ctypes.byref(params), n, cap, ptr(pr.mean2d), ptr(pr.cov2d),
@@ -382,15 +397,70 @@ def _pipeline(device) -> ViewPipeline:
     return _pipelines[key]
 
 
+_copy_streams: dict = {}
+
+
+def _copy_stream(device) -> torch.cuda.Stream:
+    key = (device.type, device.index)
+    if key not in _copy_streams:
+        _copy_streams[key] = torch.cuda.Stream(device)
+    return _copy_streams[key]
+
+
+def _upload_overlapped(host, consts, device):
+    """Copy the camera constants and the host parameters (mean, qvec,
+    log_scale, sh, alpha_logit) to `device` on a copy stream: constants and
+    the four geometry tensors first, then the SH coefficients.  The current
+    stream waits only for the first group, so projection and binning run
+    while the SH coefficients (the bulk of the bytes) are still in flight;
+    nothing else is copied host->device before the raster, so no copy on the
+    current stream queues behind them.  Returns the device tensors, the
+    device constants and the event the raster stage must wait for."""
+    main = torch.cuda.current_stream(device)
+    cs = _copy_stream(device)
+    dev_t = [torch.empty(h.shape, dtype=h.dtype, device=device) for h in host]
+    dev_c = torch.empty(consts.shape, dtype=consts.dtype, device=device)
+    cs.wait_stream(main)  # the fresh buffers may reuse memory the main stream still reads
+    geo_done = torch.cuda.Event()
+    sh_done = torch.cuda.Event()
+    with torch.cuda.stream(cs):
+        for d, h in [(dev_c, consts)] + [(dev_t[k], host[k]) for k in (0, 1, 2, 4, 3)]:
+            d.copy_(h, non_blocking=True)
+            d.record_stream(cs)
+            if d is dev_t[4]:
+                geo_done.record(cs)
+        sh_done.record(cs)
+    main.wait_event(geo_done)
+    return dev_t, dev_c, sh_done
+
+
 class FusedRender(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, mean, qvec, log_scale, sh, alpha_logit, c2w_np, cam, settings, aux=None):
-        for x, name in ((mean, "mean"), (qvec, "qvec"), (log_scale, "log_scale"), (sh, "sh_coeffs"),
-                        (alpha_logit, "alpha_logit")):
-            check_tensor(x, name)
+    def forward(ctx, mean, qvec, log_scale, sh, alpha_logit, c2w_np, cam, settings, aux=None, device=None):
+        host_mode = not mean.is_cuda
+        names = ("mean", "qvec", "log_scale", "sh_coeffs", "alpha_logit")
+        tensors = (mean, qvec, log_scale, sh, alpha_logit)
+        sh_ready = cam_consts = None
+        if host_mode:
+            # host-resident parameters: uploaded every call, overlapped with
+            # projection and binning; gradients come back to the host
+            for x, name in zip(tensors, names):
+                check_tensor(x, name, cuda=False)
+                if x.is_cuda:
+                    raise RuntimeError(f"{name} must be on the host like mean")
+            dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+            with torch.cuda.device(dev):
+                (mean, qvec, log_scale, sh, alpha_logit), cam_consts, sh_ready = _upload_overlapped(
+                    tensors, camera_consts(c2w_np, cam), dev)
+        else:
+            for x, name in zip(tensors, names):
+                check_tensor(x, name)
         pipe = _pipeline(mean.device)
-        state = pipe.forward(mean, qvec, log_scale, sh, alpha_logit, c2w_np, cam, settings)
+        with torch.cuda.device(mean.device):
+            state = pipe.forward(mean, qvec, log_scale, sh, alpha_logit, c2w_np, cam, settings, sh_ready=sh_ready,
+                                 cam_consts=cam_consts)
         ctx.save_for_backward(mean, qvec, log_scale, sh, alpha_logit)
+        ctx.host_mode = host_mode
         ctx.state = state
         ctx.pipe = pipe
         ctx.aux = aux
@@ -403,15 +473,22 @@ class FusedRender(torch.autograd.Function):
     @staticmethod
     def backward(ctx, grad_out):
         mean, qvec, log_scale, sh, alpha_logit = ctx.saved_tensors
-        grads = ctx.pipe.backward(ctx.state, mean, qvec, log_scale, sh, alpha_logit, grad_out)
+        with torch.cuda.device(mean.device):
+            grads = ctx.pipe.backward(ctx.state, mean, qvec, log_scale, sh, alpha_logit, grad_out)
+            if ctx.host_mode:  # gradients of host parameters live on the host
+                host = tuple(torch.empty(g.shape, dtype=g.dtype, pin_memory=True) for g in grads)
+                for h, g in zip(host, grads):
+                    h.copy_(g, non_blocking=True)
+                torch.cuda.current_stream(mean.device).synchronize()
+                grads = host
         if ctx.aux is not None:
             ctx.aux["mean2d_grad"] = ctx.state["g_mean2d"]
         ctx.state = None
-        return grads + (None, None, None, None)
+        return grads + (None, None, None, None, None)
 
 
 def rasterize(mean, qvec, log_scale, sh_coeffs, alpha_logit, c2w, cam: CameraInfo,
-              settings: RasterSettings | None = None, aux: dict | None = None) -> torch.Tensor:
+              settings: RasterSettings | None = None, aux: dict | None = None, device=None) -> torch.Tensor:
     """Render one view: parameters as in SHRenderer (log-scales, opacity
     logits, SH [N,3,C_max^2]) and a [3,4] camera-to-world (host array or
     tensor).  Returns the [H,W,3] image; differentiable w.r.t. all five
@@ -421,9 +498,15 @@ def rasterize(mean, qvec, log_scale, sh_coeffs, alpha_logit, c2w, cam: CameraInf
     with ``settings.output_maps`` also the alpha (1 - final transmittance) and
     depth (sum of T a G z) maps (``aux["alpha_map"]``, ``aux["depth_map"]``,
     [H,W], not differentiated).  ``settings.bg`` composites a background
-    colour behind the Gaussians (the gradients include it)."""
+    colour behind the Gaussians (the gradients include it).
+
+    Host-resident parameters (CPU tensors, pinned for overlap) are uploaded
+    to ``device`` (default: the current CUDA device) on every call, the SH
+    coefficients overlapped with projection and binning; the image is
+    returned on the device and the backward returns the parameters'
+    gradients on the host (pinned)."""
     settings = settings or RasterSettings()
     if isinstance(c2w, torch.Tensor):
         c2w = c2w.detach().to("cpu", torch.float32).numpy()
     return FusedRender.apply(mean, qvec, log_scale, sh_coeffs, alpha_logit, np.asarray(c2w, np.float32), cam,
-                             settings, aux)
+                             settings, aux, device)
