@@ -259,10 +259,11 @@ struct SmemLayout {
   int *ids;
   float *inv_det;  // 1 / det(cov), backward only
   float *zdep;     // camera depth, forward with a depth map only
+  float *rq;       // skip radius R of the ellipse test (inf: no ellipse test)
   float *sh;
 };
 
-constexpr int kRecordFloats = 12;  // floats of per-Gaussian records per batch slot
+constexpr int kRecordFloats = 13;  // floats of per-Gaussian records per batch slot
 
 // Shared-memory layout of one batch of B Gaussians (B a multiple of 4):
 // kRecordFloats*B floats of records followed by the SH rows (16-byte aligned).
@@ -276,6 +277,7 @@ __device__ __forceinline__ SmemLayout carve(float *smem, int B) {
   L.ids = reinterpret_cast<int *>(smem + 9 * B);
   L.inv_det = smem + 10 * B;
   L.zdep = smem + 11 * B;
+  L.rq = smem + 12 * B;
   L.sh = smem + kRecordFloats * B;
   return L;
 }
@@ -291,9 +293,12 @@ __device__ __forceinline__ float inf_f() { return __int_as_float(0x7f800000); }
 // is skipped; that ellipse lies inside the box |dx| <= sqrt(R c0),
 // |dy| <= sqrt(R c3), widened by 1 % more.  drop = the Gaussian is skipped by
 // every pixel (a < 1/255 with a finite, non-negative G).  Anything else gets
-// an infinite box and takes the exact per-pixel path.
-__device__ __forceinline__ float2 skip_box(float4 cv, float2 m, float a, bool &drop) {
+// an infinite box and takes the exact per-pixel path.  `rq` receives R for
+// the ellipse test of ellipse_meets_block when the two off-diagonal entries
+// agree (as a projected covariance's do up to rounding), else +inf.
+__device__ __forceinline__ float2 skip_box(float4 cv, float2 m, float a, bool &drop, float &rq) {
   drop = false;
+  rq = inf_f();
   const bool finite = isfinite(cv.x) && isfinite(cv.y) && isfinite(cv.z) && isfinite(cv.w) &&
                       isfinite(m.x) && isfinite(m.y);
   const float det = fmaf(cv.x, cv.w, -(cv.y * cv.z));
@@ -304,7 +309,35 @@ __device__ __forceinline__ float2 skip_box(float4 cv, float2 m, float a, bool &d
     return make_float2(0.0f, 0.0f);
   }
   const float R = fmaxf(2.0f * logf(255.0f * a), 0.0f) * 1.01f + 0.05f;
+  if (fabsf(cv.y - cv.z) <= 1e-4f * sqrtf(cv.x * cv.w)) rq = R;
   return make_float2(sqrtf(R * cv.x) * 1.01f + 1e-6f, sqrtf(R * cv.w) * 1.01f + 1e-6f);
+}
+
+// Conservative test that some point of the block [blk.x, blk.y] x [blk.z,
+// blk.w] (the warp's pixel centres) lies inside the ellipse where the pair can
+// reach 1/255: min over the block of the quadratic form of the radial,
+// (c3 x^2 - (c1 + c2) x y + c0 y^2) / det, is at most R.  The form is positive
+// definite for the covariances skip_box hands an R (c0, c3 > 0, det > 1e-2
+// c0 c3, c1 ~ c2), so when the centre lies outside the block the minimum is on
+// its boundary, found exactly per edge (clamped stationary point).  Float error
+// of the form is far below the 1 % widening of R; an extra 0.1 % is added.
+__device__ __forceinline__ bool ellipse_meets_block(float4 cv, float2 m, float R, float4 blk) {
+  const float X0 = blk.x - m.x, X1 = blk.y - m.x, Y0 = blk.z - m.y, Y1 = blk.w - m.y;
+  if (X0 <= 0.0f && X1 >= 0.0f && Y0 <= 0.0f && Y1 >= 0.0f) return true;
+  const float A = cv.w, Cc = cv.x, H = 0.5f * (cv.y + cv.z);
+  const float det = fmaf(cv.x, cv.w, -(cv.y * cv.z));
+  const float lim = R * det * 1.001f;
+  float best = inf_f();
+#pragma unroll
+  for (int e = 0; e < 2; ++e) {
+    const float X = e ? X1 : X0;
+    const float y = fminf(fmaxf(H * X / Cc, Y0), Y1);
+    best = fminf(best, fmaf(A * X, X, fmaf(-2.0f * H * X, y, Cc * y * y)));
+    const float Y = e ? Y1 : Y0;
+    const float x = fminf(fmaxf(H * Y / A, X0), X1);
+    best = fminf(best, fmaf(A * x, x, fmaf(-2.0f * H * x, Y, Cc * Y * Y)));
+  }
+  return best <= lim;
 }
 
 __device__ __forceinline__ unsigned lanemask_lt() {
@@ -392,7 +425,7 @@ __device__ __forceinline__ int load_batch(const RasterArgs &a, const ViewCtx &ct
   int id = -1;
   float2 mm = make_float2(0.0f, 0.0f), box = make_float2(0.0f, 0.0f);
   float4 cv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  float al = 0.0f;
+  float al = 0.0f, rq = 0.0f;
   if (t < nb) {
     id = a.ids[first + t];
     if (id >= ctx.item_lo && id < ctx.item_hi) {
@@ -402,7 +435,7 @@ __device__ __forceinline__ int load_batch(const RasterArgs &a, const ViewCtx &ct
       cv = make_float4(c[0], c[1], c[2], c[3]);
       al = fminf(a.alpha[id], 0.99f);
       bool drop;
-      box = skip_box(cv, mm, al, drop);
+      box = skip_box(cv, mm, al, drop, rq);
       keep = !drop && !(mm.x + box.x < tx0) && !(mm.x - box.x > tx1) && !(mm.y + box.y < ty0) &&
              !(mm.y - box.y > ty1);
     }
@@ -425,6 +458,7 @@ __device__ __forceinline__ int load_batch(const RasterArgs &a, const ViewCtx &ct
     L.cov[pos] = cv;
     L.alpha[pos] = al;
     L.box[pos] = box;
+    L.rq[pos] = rq;
     if constexpr (INV_DET) L.inv_det[pos] = 1.0f / fmaf(cv.x, cv.w, -(cv.y * cv.z));
     if constexpr (DEPTH) {
       if (a.depth_out) L.zdep[pos] = a.depth[id];
@@ -482,8 +516,9 @@ __device__ __forceinline__ float4 warp_block(float px, float py) {
 }
 
 // This warp's list of the batch Gaussians (batch positions, in order) whose
-// skip box meets the warp's pixel block; the others are skipped by every
-// lane of the warp, so leaving them out changes nothing.  All lanes call it.
+// skip box, and skip ellipse where there is one, meet the warp's pixel
+// block; the others are skipped by every lane of the warp, so leaving them
+// out changes nothing.  All lanes call it.
 __device__ __forceinline__ int warp_list(const SmemLayout &L, int nk, float4 blk, int *wl,
                                          int lane) {
   int cnt = 0;
@@ -494,6 +529,10 @@ __device__ __forceinline__ int warp_list(const SmemLayout &L, int nk, float4 blk
       const float2 m = L.mean[i], h = L.box[i];
       hit = !(m.x + h.x < blk.x) && !(m.x - h.x > blk.y) && !(m.y + h.y < blk.z) &&
             !(m.y - h.y > blk.w);
+      if (hit) {
+        const float R = L.rq[i];
+        if (R < inf_f()) hit = ellipse_meets_block(L.cov[i], m, R, blk);
+      }
     }
     const unsigned b = __ballot_sync(kFull, hit);
     if (hit) wl[cnt + __popc(b & lanemask_lt())] = i;
