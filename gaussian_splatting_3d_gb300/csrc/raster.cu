@@ -319,8 +319,10 @@ __device__ __forceinline__ float2 skip_box(float4 cv, float2 m, float a, bool &d
 // (c3 x^2 - (c1 + c2) x y + c0 y^2) / det, is at most R.  The form is positive
 // definite for the covariances skip_box hands an R (c0, c3 > 0, det > 1e-2
 // c0 c3, c1 ~ c2), so when the centre lies outside the block the minimum is on
-// its boundary, found exactly per edge (clamped stationary point).  Float error
-// of the form is far below the 1 % widening of R; an extra 0.1 % is added.
+// its boundary, found per edge at the clamped stationary point.  Float error
+// of the form is far below the 1 % widening of R; an extra 0.1 % is added,
+// which also covers the approximate division of the stationary point (the
+// form is flat there: an offset d raises it by c d^2, relative 2^-40 or less).
 __device__ __forceinline__ bool ellipse_meets_block(float4 cv, float2 m, float R, float4 blk) {
   const float X0 = blk.x - m.x, X1 = blk.y - m.x, Y0 = blk.z - m.y, Y1 = blk.w - m.y;
   if (X0 <= 0.0f && X1 >= 0.0f && Y0 <= 0.0f && Y1 >= 0.0f) return true;
@@ -331,10 +333,10 @@ __device__ __forceinline__ bool ellipse_meets_block(float4 cv, float2 m, float R
 #pragma unroll
   for (int e = 0; e < 2; ++e) {
     const float X = e ? X1 : X0;
-    const float y = fminf(fmaxf(H * X / Cc, Y0), Y1);
+    const float y = fminf(fmaxf(__fdividef(H * X, Cc), Y0), Y1);
     best = fminf(best, fmaf(A * X, X, fmaf(-2.0f * H * X, y, Cc * y * y)));
     const float Y = e ? Y1 : Y0;
-    const float x = fminf(fmaxf(H * Y / A, X0), X1);
+    const float x = fminf(fmaxf(__fdividef(H * Y, A), X0), X1);
     best = fminf(best, fmaf(A * x, x, fmaf(-2.0f * H * x, Y, Cc * Y * Y)));
   }
   return best <= lim;
