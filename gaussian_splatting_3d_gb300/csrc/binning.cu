@@ -36,7 +36,7 @@ constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kCountMask = (1u << 30) - 1u;
 constexpr uint32_t kSpinLimit = 1u << 22;
-constexpr int kEmitItems = 8;
+constexpr int kEmitItems = 2;
 constexpr int kEmitTile = kThreads * kEmitItems;
 constexpr unsigned long long kFlag64Agg = 1ull << 62;
 constexpr unsigned long long kFlag64Prefix = 2ull << 62;
@@ -234,12 +234,15 @@ __device__ __forceinline__ long long rect_count(const int32_t *tl, const int32_t
 }
 
 // Exclusive scan of key counts in depth order (decoupled look-back over
-// chunks of 2048 Gaussians) fused with the emission of (tile, Gaussian)
-// pairs.  Warp w of a chunk owns its items w*256 + j*32 + lane (j = 0..7), so
-// item loads are coalesced; per group j the warp scans the 32 counts and then
-// writes the group's keys cooperatively, lane l taking keys l, l+32, ... of
-// the group (the owner item found by a 5-step search), so key writes are
-// coalesced too.  The last chunk writes the key total.
+// chunks of kEmitTile = 512 Gaussians) fused with the emission of (tile,
+// Gaussian) pairs.  Warp w of a chunk owns its items w*64 + j*32 + lane
+// (j = 0, 1), so item loads are coalesced; per group j the warp scans the 32
+// counts and then writes the group's keys cooperatively, lane l taking keys
+// l, l+32, ... of the group (the owner item found by a 5-step search), so key
+// writes are coalesced too.  Chunks are small because the key count per
+// Gaussian falls steeply with depth: the nearest chunks carry most keys, and
+// smaller chunks spread them over more CTAs.  The last chunk writes the key
+// total.
 __global__ void __launch_bounds__(kThreads)
     emit_kernel(const uint32_t *__restrict__ order, uint32_t n,
                 const int32_t *__restrict__ rect_tl, const int32_t *__restrict__ rect_br,
@@ -295,37 +298,50 @@ __global__ void __launch_bounds__(kThreads)
     if (k < w) warp_off += c;
     block_total += c;
   }
-  if (t == 0) {
+  if (w == 0) {
+    // decoupled look-back, 32 predecessors per poll: lane l reads chunk
+    // c - l; the nearest inclusive prefix ends the walk, the aggregates of
+    // the chunks before it are summed with the prefix.
     unsigned long long prev = 0;
     unsigned long long *mine = status + chunk;
     if (chunk == 0) {
-      st_volatile64(mine, kFlag64Prefix | block_total);
+      if (lane == 0) st_volatile64(mine, kFlag64Prefix | block_total);
     } else {
-      st_volatile64(mine, kFlag64Agg | block_total);
+      if (lane == 0) st_volatile64(mine, kFlag64Agg | block_total);
       int64_t c = (int64_t)chunk - 1;
       uint32_t spins = 0;
-      while (c >= 0) {
-        const unsigned long long sv = ld_volatile64(status + c);
+      while (true) {
+        const int64_t idx = c - lane;
+        const unsigned long long sv = idx >= 0 ? ld_volatile64(status + idx) : kFlag64Prefix;
         const unsigned long long flag = sv & ~kCount64Mask;
-        if (flag == 0ull) {
+        const uint32_t pmask = __ballot_sync(0xffffffffu, flag == kFlag64Prefix);
+        const uint32_t zmask = __ballot_sync(0xffffffffu, flag == 0ull);
+        const int first = pmask ? __ffs(pmask) - 1 : 31;  // last lane the walk needs
+        const uint32_t need = first == 31 ? 0xffffffffu : ((2u << first) - 1u);
+        if (zmask & need) {  // a needed predecessor has not published yet
           if (++spins > kSpinLimit) {
-            atomicOr(error, kErrTimeout);
+            if (lane == 0) atomicOr(error, kErrTimeout);
             break;
           }
           __nanosleep(32);
           continue;
         }
-        prev += sv & kCount64Mask;
-        if (flag == kFlag64Prefix) break;
-        --c;
+        unsigned long long v = lane <= first ? (sv & kCount64Mask) : 0ull;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        prev += v;
+        if (pmask) break;
+        c -= 32;
       }
-      st_volatile64(mine, kFlag64Prefix | (prev + block_total));
+      if (lane == 0) st_volatile64(mine, kFlag64Prefix | (prev + block_total));
     }
-    s_prefix = prev;
-    if ((unsigned long long)(chunk + 1) * kEmitTile >= n) {
-      const unsigned long long total = prev + block_total;
-      *total_out = total;
-      *k_eff = (uint32_t)(total < capacity ? total : capacity);
+    if (lane == 0) {
+      s_prefix = prev;
+      if ((unsigned long long)(chunk + 1) * kEmitTile >= n) {
+        const unsigned long long total = prev + block_total;
+        *total_out = total;
+        *k_eff = (uint32_t)(total < capacity ? total : capacity);
+      }
     }
   }
   __syncthreads();
