@@ -434,17 +434,25 @@ __global__ void ranges_kernel(const uint32_t *__restrict__ tiles, const uint32_t
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// Binning workspace.  Everything that must start at zero -- the chunk
+// tickets, the status block, the digit histograms and every pass's look-back
+// flags -- sits in one contiguous region (`zero_begin`, cleared by a single
+// memset per call up to the last pass in use); each pass owns its own
+// look-back flags and ticket, so nothing is cleared between passes.
+constexpr int kMaxPasses = 4;  // 8-bit digits of a 32-bit key
 struct Workspace {
   uint32_t *dkeys[2], *dvals[2];
   uint32_t *tkeys[2], *tvals[2];
-  uint32_t *hist;      // [8][256]
-  uint32_t *status;    // [max_chunks][256]
-  unsigned long long *emit_status;
-  uint32_t *counters;  // [16]
+  char *zero_begin;
+  uint32_t *counters;  // [16]: depth passes 0-3, tile passes 4-7, emission 8
   uint32_t *error;
   unsigned long long *total;
   uint32_t *k_eff;  // min(total, capacity), the key count the tile sort uses
-  size_t status_words, emit_words;
+  uint32_t *hist;   // [8][256]: depth digits 0-3, tile digits 4-7
+  unsigned long long *emit_status;
+  uint32_t *status_depth;  // [kMaxPasses][depth_chunks][256]
+  uint32_t *status_tile;   // [kMaxPasses][tile_chunks][256]
+  size_t depth_chunks, tile_chunks, emit_words;
   size_t bytes;
 };
 
@@ -462,12 +470,8 @@ Workspace carve_ws(void *base, int64_t n, int64_t cap) {
   for (int i = 0; i < 2; ++i) w.dvals[i] = reinterpret_cast<uint32_t *>(take(4 * nn));
   for (int i = 0; i < 2; ++i) w.tkeys[i] = reinterpret_cast<uint32_t *>(take(4 * cc));
   for (int i = 0; i < 2; ++i) w.tvals[i] = reinterpret_cast<uint32_t *>(take(4 * cc));
-  w.hist = reinterpret_cast<uint32_t *>(take(8 * 256 * 4));
-  const size_t max_items = nn > cc ? nn : cc;
-  w.status_words = ((max_items + kTile - 1) / kTile) * 256;
-  w.status = reinterpret_cast<uint32_t *>(take(4 * w.status_words));
-  w.emit_words = (nn + kEmitTile - 1) / kEmitTile;
-  w.emit_status = reinterpret_cast<unsigned long long *>(take(8 * w.emit_words));
+  // zero-initialised region, in the order the passes use it
+  w.zero_begin = take(0);
   w.counters = reinterpret_cast<uint32_t *>(take(16 * 4));
   // the status block: key total (u64), error bits (u32), key count used (u32),
   // 16 contiguous bytes that one copy brings back
@@ -475,6 +479,13 @@ Workspace carve_ws(void *base, int64_t n, int64_t cap) {
   w.total = reinterpret_cast<unsigned long long *>(status_block);
   w.error = reinterpret_cast<uint32_t *>(status_block ? status_block + 8 : nullptr);
   w.k_eff = reinterpret_cast<uint32_t *>(status_block ? status_block + 12 : nullptr);
+  w.hist = reinterpret_cast<uint32_t *>(take(8 * 256 * 4));
+  w.emit_words = (nn + kEmitTile - 1) / kEmitTile;
+  w.emit_status = reinterpret_cast<unsigned long long *>(take(8 * w.emit_words));
+  w.depth_chunks = (nn + kTile - 1) / kTile;
+  w.status_depth = reinterpret_cast<uint32_t *>(take(4 * 256 * kMaxPasses * w.depth_chunks));
+  w.tile_chunks = (cc + kTile - 1) / kTile;
+  w.status_tile = reinterpret_cast<uint32_t *>(take(4 * 256 * kMaxPasses * w.tile_chunks));
   w.bytes = off;
   return w;
 }
@@ -482,33 +493,36 @@ Workspace carve_ws(void *base, int64_t n, int64_t cap) {
 // Stable LSD sort of n (key, value) pairs over `bits` low key bits; the count
 // is n_max, or *n_dev (at most n_max) when n_dev is given.  The final pass
 // writes into (final_keys, final_vals); intermediate passes use the two
-// scratch buffers.  keys_in/vals_in are never written.
+// scratch buffers.  keys_in/vals_in are never written.  `hist` (4 x 256
+// digit counts), `tickets` (4 chunk counters) and `status` (4 passes of
+// `chunks_cap` look-back rows) must be zero on entry.
 int radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t n_max,
                const uint32_t *n_dev, int bits, uint32_t *scratch_k[2], uint32_t *scratch_v[2],
-               uint32_t *final_keys, uint32_t *final_vals, const Workspace &w, cudaStream_t s) {
+               uint32_t *final_keys, uint32_t *final_vals, uint32_t *hist, uint32_t *tickets,
+               uint32_t *status, size_t chunks_cap, uint32_t *error, cudaStream_t s) {
   const int passes = (bits + 7) / 8;
   if (n_max == 0 || passes == 0) return GSX_OK;
-  cudaError_t e = cudaMemsetAsync(w.hist, 0, 8 * 256 * 4, s);
-  if (e != cudaSuccess) return cuda_status(e, "memset histogram");
   uint32_t hist_grid = (n_max + kThreads * 16 - 1) / (kThreads * 16);
   if (hist_grid > 1024u) hist_grid = 1024u;
   count_launches(1);
-  histogram_kernel<<<hist_grid, kThreads, 0, s>>>(keys_in, n_max, n_dev, passes, w.hist);
-  e = cudaGetLastError();
+  histogram_kernel<<<hist_grid, kThreads, 0, s>>>(keys_in, n_max, n_dev, passes, hist);
+  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_status(e, "histogram_kernel launch");
   const uint32_t chunks = (n_max + kTile - 1) / kTile;
+  if (chunks > chunks_cap) {
+    set_error("radix sort of %u keys needs %u chunks, the workspace holds %zu", n_max, chunks,
+              chunks_cap);
+    return GSX_ERR_CAPACITY;
+  }
   const uint32_t *ki = keys_in, *vi = vals_in;
   for (int p = 0; p < passes; ++p) {
     const bool last = p == passes - 1;
     uint32_t *ko = last ? final_keys : scratch_k[p & 1];
     uint32_t *vo = last ? final_vals : scratch_v[p & 1];
-    e = cudaMemsetAsync(w.status, 0, (size_t)chunks * 256 * 4, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(w.counters + p, 0, 4, s);
-    if (e != cudaSuccess) return cuda_status(e, "memset look-back status");
     count_launches(1);
     onesweep_kernel<<<chunks, kThreads, 0, s>>>(ki, vi, ko, vo, n_max, n_dev, 8 * p,
-                                                 w.hist + 256 * p, w.status, w.counters + p,
-                                                 w.error);
+                                                 hist + 256 * p, status + chunks_cap * 256 * p,
+                                                 tickets + p, error);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e, "onesweep_kernel launch");
     ki = ko;
@@ -544,23 +558,25 @@ int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
     set_error("binning workspace too small: %zu < %zu bytes", ws_bytes, w.bytes);
     return GSX_ERR_CAPACITY;
   }
+  const int tile_bits = bits_for((uint64_t)(n_tiles > 0 ? n_tiles - 1 : 0));
+  const int tile_passes = (tile_bits + 7) / 8;
+  // one clear of the zero-initialised state, through the last tile pass in use
+  const char *zero_end = reinterpret_cast<const char *>(w.status_tile) +
+                         (size_t)4 * 256 * tile_passes * w.tile_chunks;
   cudaError_t e = cudaMemsetAsync(start, 0xff, sizeof(int32_t) * (size_t)n_tiles, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(end, 0xff, sizeof(int32_t) * (size_t)n_tiles, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(w.counters, 0, 16 * 4, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(w.total, 0, kStatusBlockBytes, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.zero_begin, 0, (size_t)(zero_end - w.zero_begin), s);
   if (e != cudaSuccess) return cuda_status(e, "memset binning state");
   if (n == 0) return GSX_OK;
   const uint32_t nn = (uint32_t)n;
   // 1. Gaussians sorted by depth bits (values = Gaussian index)
   uint32_t *sk[2] = {w.dkeys[0], w.dkeys[1]}, *sv[2] = {w.dvals[0], w.dvals[1]};
   int st = radix_sort(reinterpret_cast<const uint32_t *>(depth), nullptr, nn, nullptr, 32, sk, sv,
-                      w.dkeys[1], w.dvals[1], w, s);
+                      w.dkeys[1], w.dvals[1], w.hist, w.counters, w.status_depth, w.depth_chunks,
+                      w.error, s);
   if (st != GSX_OK) return st;
   // 2. scan of counts + emission
   const uint32_t emit_chunks = (nn + kEmitTile - 1) / kEmitTile;
-  e = cudaMemsetAsync(w.emit_status, 0, 8 * (size_t)emit_chunks, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(w.counters + 8, 0, 4, s);
-  if (e != cudaSuccess) return cuda_status(e, "memset emission state");
   count_launches(1);
   emit_kernel<<<emit_chunks, kThreads, 0, s>>>(
       w.dvals[1], nn, rect_tl, rect_br, rect_stride, counts, n_tiles_w, n_tiles_h, views, n_views,
@@ -575,7 +591,6 @@ int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
   // tkeys[1] for even p and tkeys[0] for odd p; the last pass writes the ids
   // into the caller's buffer and its keys into whichever tile buffer is not
   // its input.
-  const int tile_bits = bits_for((uint64_t)(n_tiles - 1));
   uint32_t *ids_u = reinterpret_cast<uint32_t *>(ids);
   uint32_t *final_keys = w.tkeys[0];
   if (tile_bits == 0) {
@@ -585,8 +600,8 @@ int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
     const int passes = (tile_bits + 7) / 8;
     uint32_t *tk[2] = {w.tkeys[1], w.tkeys[0]}, *tv[2] = {w.tvals[1], w.tvals[0]};
     final_keys = (passes & 1) ? w.tkeys[1] : w.tkeys[0];
-    st = radix_sort(w.tkeys[0], w.tvals[0], cap, w.k_eff, tile_bits, tk, tv, final_keys, ids_u, w,
-                    s);
+    st = radix_sort(w.tkeys[0], w.tvals[0], cap, w.k_eff, tile_bits, tk, tv, final_keys, ids_u,
+                    w.hist + 4 * 256, w.counters + 4, w.status_tile, w.tile_chunks, w.error, s);
     if (st != GSX_OK) return st;
   }
   // 4. start / end
