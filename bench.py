@@ -175,7 +175,7 @@ def run_gsx(args):
     pipe = renderer.ViewPipeline(dev)
 
     def step(timer=None):
-        state = pipe.forward(*params, view.c2w, view.cam, settings, timer=timer)
+        state = pipe.forward(*params, view.c2w, view.cam, settings, timer=timer, prepare_grads=True)
         grads = pipe.backward(state, *params, W, timer=timer)
         return state, grads
 

@@ -253,11 +253,16 @@ class ViewPipeline:
         self.key_capacity = 0  # grows to ~1.25x the largest key count seen
 
     def forward(self, mean, qvec, log_scale, sh, alpha_logit, c2w_np, cam: CameraInfo,
-                settings: RasterSettings, timer=None, sh_ready=None, cam_consts=None):
+                settings: RasterSettings, timer=None, sh_ready=None, cam_consts=None,
+                prepare_grads: bool = False):
         """``sh_ready``: an event the raster stage waits for (the SH
         coefficients still arriving on a copy stream while projection and
         binning run); ``cam_consts``: the device copy of
-        ``camera_consts(c2w_np, cam)`` when the caller uploaded it."""
+        ``camera_consts(c2w_np, cam)`` when the caller uploaded it;
+        ``prepare_grads``: a backward will follow, so its zeroed gradient
+        accumulators are filled on a side stream while the raster forward
+        runs (not in the memory mode, which holds nothing extra between the
+        passes)."""
         dev = mean.device
         n = mean.shape[0]
         sh_stride = sh.shape[-1]
@@ -272,10 +277,14 @@ class ViewPipeline:
         topleft, c2w_dev = cam_consts[:2], cam_consts[2:]
         out = torch.empty((cam.h, cam.w, 3), dtype=torch.float32, device=dev)
         params = _raster_params(cam, settings, C, sh_stride)
+        grads = grads_ready = None
         cap = max(self.key_capacity, 1 << 16)
         for _ in range(3):
             with ev("binning"):
                 ids, start, end = bin_gaussians_async(pr, ntw, nth, cap)
+            if prepare_grads and grads is None and not settings.recompute_projection:
+                # after the binning (whose working set lives in L2), beside the raster
+                grads, grads_ready = _zeroed_grad_buffers(dev, n, sh)
             if sh_ready is not None:  # only the raster reads the SH coefficients
                 torch.cuda.current_stream(dev).wait_event(sh_ready)
             with ev("raster_fwd"):
@@ -315,6 +324,8 @@ class ViewPipeline:
                   counts=visible_counts)
         if settings.output_maps:
             st["alpha_map"], st["depth_map"] = maps
+        if grads is not None:
+            st["grads"], st["grads_ready"] = grads, grads_ready
         return st
 
     def backward(self, state, mean, qvec, log_scale, sh, alpha_logit, grad_out, timer=None):
@@ -326,10 +337,14 @@ class ViewPipeline:
             with ev("project_recompute"):
                 pr = project(mean, qvec, log_scale, alpha_logit, state["gcam"], state["settings"])
         grad_out = grad_out.contiguous()
-        g_mean2d = torch.zeros((n, 2), dtype=torch.float32, device=dev)
-        g_cov2d = torch.zeros((n, 4), dtype=torch.float32, device=dev)
-        g_alpha = torch.zeros((n,), dtype=torch.float32, device=dev)
-        g_sh = torch.zeros_like(sh)
+        if state.get("grads") is not None and state["grads"][3].shape == sh.shape:
+            torch.cuda.current_stream(dev).wait_event(state["grads_ready"])
+            g_mean2d, g_cov2d, g_alpha, g_sh = state.pop("grads")
+        else:
+            g_mean2d = torch.zeros((n, 2), dtype=torch.float32, device=dev)
+            g_cov2d = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+            g_alpha = torch.zeros((n,), dtype=torch.float32, device=dev)
+            g_sh = torch.zeros_like(sh)
         with ev("raster_bwd"):
             _lib.call("gsx_render_backward", ctypes.byref(state["params"]), n, state["cap"], ptr(pr.mean2d),
                       ptr(pr.cov2d), ptr(sh), ptr(pr.alpha), ptr(state["start"]), ptr(state["end"]),
@@ -398,6 +413,32 @@ def _pipeline(device) -> ViewPipeline:
 
 
 _copy_streams: dict = {}
+_fill_streams: dict = {}
+
+
+def _zeroed_grad_buffers(device, n: int, sh: torch.Tensor):
+    """The raster backward's accumulators (dL/dmean2d [n,2], dL/dcov2d [n,4],
+    dL/dalpha [n], dL/dsh like sh), zero-filled on a side stream that starts
+    after the work already queued on the current stream; returns them and
+    the event the backward waits for."""
+    main = torch.cuda.current_stream(device)
+    key = (device.type, device.index)
+    if key not in _fill_streams:
+        _fill_streams[key] = torch.cuda.Stream(device)
+    fs = _fill_streams[key]
+    bufs = (torch.empty((n, 2), dtype=torch.float32, device=device),
+            torch.empty((n, 4), dtype=torch.float32, device=device),
+            torch.empty((n,), dtype=torch.float32, device=device),
+            torch.empty(sh.shape, dtype=sh.dtype, device=device))
+    fs.wait_stream(main)  # the fresh blocks may still be read by queued work
+    done = torch.cuda.Event()
+    with torch.cuda.stream(fs):
+        for b in bufs:
+            b.zero_()
+            b.record_stream(fs)
+        done.record(fs)
+    return bufs, done
+
 
 
 def _copy_stream(device) -> torch.cuda.Stream:
@@ -458,7 +499,7 @@ class FusedRender(torch.autograd.Function):
         pipe = _pipeline(mean.device)
         with torch.cuda.device(mean.device):
             state = pipe.forward(mean, qvec, log_scale, sh, alpha_logit, c2w_np, cam, settings, sh_ready=sh_ready,
-                                 cam_consts=cam_consts)
+                                 cam_consts=cam_consts, prepare_grads=any(ctx.needs_input_grad[:5]))
         ctx.save_for_backward(mean, qvec, log_scale, sh, alpha_logit)
         ctx.host_mode = host_mode
         ctx.state = state
