@@ -420,16 +420,39 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// start/end of every tile from the sorted tile ids: 4 consecutive keys per
+// thread (one 16-byte load; `tiles` is 16-byte aligned), their neighbours
+// from the adjacent threads' loads or, at warp edges, from memory.
 __global__ void ranges_kernel(const uint32_t *__restrict__ tiles, const uint32_t *__restrict__ K_dev,
                               uint32_t n_tiles, int32_t *__restrict__ start,
                               int32_t *__restrict__ end) {
   const uint32_t K = *K_dev;
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= K) return;
-  const uint32_t t = tiles[i];
-  if (t >= n_tiles) return;
-  if (i == 0 || tiles[i - 1] != t) start[t] = (int32_t)i;
-  if (i == K - 1 || tiles[i + 1] != t) end[t] = (int32_t)(i + 1);
+  const uint32_t base = 4u * (blockIdx.x * blockDim.x + threadIdx.x);
+  if (base >= K) return;
+  uint32_t v[4];
+  if (base + 4 <= K) {
+    const uint4 q = *reinterpret_cast<const uint4 *>(tiles + base);
+    v[0] = q.x;
+    v[1] = q.y;
+    v[2] = q.z;
+    v[3] = q.w;
+  } else {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) v[j] = base + j < K ? tiles[base + j] : 0xffffffffu;
+  }
+  const uint32_t prev = base > 0 ? tiles[base - 1] : 0xffffffffu;
+  const uint32_t next = base + 4 < K ? tiles[base + 4] : 0xffffffffu;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const uint32_t i = base + j;
+    if (i >= K) break;
+    const uint32_t t = v[j];
+    if (t >= n_tiles) continue;
+    const uint32_t before = j == 0 ? prev : v[j - 1];
+    const uint32_t after = j == 3 ? next : v[j + 1];
+    if (i == 0 || before != t) start[t] = (int32_t)i;
+    if (i == K - 1 || after != t) end[t] = (int32_t)(i + 1);
+  }
 }
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -558,6 +581,10 @@ int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
     set_error("binning workspace too small: %zu < %zu bytes", ws_bytes, w.bytes);
     return GSX_ERR_CAPACITY;
   }
+  if ((reinterpret_cast<uintptr_t>(ws) & 255) != 0) {  // the kernels use 16-byte vector loads
+    set_error("binning workspace must be 256-byte aligned");
+    return GSX_ERR_INVALID_ARG;
+  }
   const int tile_bits = bits_for((uint64_t)(n_tiles > 0 ? n_tiles - 1 : 0));
   const int tile_passes = (tile_bits + 7) / 8;
   // one clear of the zero-initialised state, through the last tile pass in use
@@ -606,8 +633,8 @@ int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
   }
   // 4. start / end
   count_launches(1);
-  ranges_kernel<<<(cap + 255) / 256, 256, 0, s>>>(final_keys, w.k_eff, (uint32_t)n_tiles, start,
-                                                   end);
+  ranges_kernel<<<(cap + 1023) / 1024, 256, 0, s>>>(final_keys, w.k_eff, (uint32_t)n_tiles, start,
+                                                     end);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_status(e, "ranges_kernel launch");
   return GSX_OK;

@@ -64,6 +64,8 @@ int gsx_culling_gaussian_bsphere(int64_t n, const float *mean, const float *qvec
 /*
  * Workspace for gsx_tile_culling_aabb_start_end and gsx_bin_gaussians:
  * n_gaussians Gaussians, up to key_capacity (tile, Gaussian) keys, n_tiles tiles.
+ * The workspace must start on a 256-byte boundary (as cudaMalloc returns);
+ * the binning calls reject others with GSX_ERR_INVALID_ARG.
  */
 size_t gsx_binning_workspace_bytes(int64_t n_gaussians, int64_t key_capacity,
                                    int64_t n_tiles);

@@ -57,3 +57,16 @@ def test_workspace_size_grows_with_capacity():
     a = lib.gsx_binning_workspace_bytes(1000, 1000, 64)
     b = lib.gsx_binning_workspace_bytes(1000, 100000, 64)
     assert b > a
+
+
+def test_unaligned_binning_workspace_is_rejected_on_the_host():
+    """The binning kernels read the workspace with 16-byte vector loads, so a
+    workspace that does not start on a 256-byte boundary is refused before
+    anything is enqueued (the pointers below are never dereferenced)."""
+    lib = _lib.load()
+    n, cap, ntw, nth = 1000, 4000, 8, 8
+    need = lib.gsx_binning_workspace_bytes(n, cap, ntw * nth)
+    fake = 1 << 40  # a non-null address; the call must return before using it
+    st = lib.gsx_bin_gaussians_async(n, fake, fake, fake, ntw, nth, cap, fake, fake, fake, fake + 16, need, None)
+    assert st == _lib.GSX_ERR_INVALID_ARG
+    assert b"256-byte aligned" in lib.gsx_last_error()
