@@ -41,14 +41,15 @@ sys.path.insert(0, ROOT)
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 
 
-def profiled_traffic(kernel: str, workload: str):
+def profiled_traffic(kernel: str, workload: str, what: str = "traffic_bytes_per_launch"):
     """DRAM bytes per launch of `kernel` (dram__bytes_read.sum +
-    dram__bytes_write.sum) from the committed ncu summary of `workload`, or
+    dram__bytes_write.sum) from the committed ncu summary of `workload` (or,
+    with what="warp_inst_per_launch", its executed warp instructions), or
     None when no capture covers it."""
     import glob
     import re
 
-    pat = re.compile(rf"^traffic_bytes_per_launch {re.escape(kernel)} {re.escape(workload)}: (\d+)\s*$")
+    pat = re.compile(rf"^{what} {re.escape(kernel)} {re.escape(workload)}: (\d+)\s*$")
     for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
         with open(path) as f:
             for line in f:
@@ -305,6 +306,17 @@ def run_gsx(args):
         line["roofline"]["traffic_source"] = f"ncu dram__bytes_read.sum + dram__bytes_write.sum, {prof[1]}"
     line["roofline"]["note"] = ("raster kernels are FP32/SFU-issue bound (see profiles/); the HBM fraction "
                                 "counts each key's Gaussian record once per tile")
+    inst = profiled_traffic(dom, args.workload, "warp_inst_per_launch") if args.n == 1_000_000 else None
+    if inst is not None and clock_info.get("sm_mhz"):
+        # the bound these kernels meet: one warp instruction per scheduler per
+        # cycle (152 SMs x 4), at the SM clock sampled during the timed region
+        n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+        peak_issue = n_sm * 4 * clock_info["sm_mhz"] * 1e6
+        got_issue = inst[0] / (stages[dom]["mean_ms"] * 1e-3)
+        line["roofline"]["issue"] = {"achieved": round(got_issue / 1e9, 1), "peak": round(peak_issue / 1e9, 1),
+                                     "unit": "G warp-inst/s", "frac": round(got_issue / peak_issue, 4),
+                                     "warp_inst_per_launch": inst[0], "source": f"ncu smsp__inst_executed.sum, "
+                                                                                f"{inst[1]}"}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(wl, args.cpu_frac)
     print(json.dumps(line), flush=True)
