@@ -14,10 +14,12 @@
 // GB300 layout: one CTA per tile, one thread per pixel, each warp an 8x4
 // block of pixels.  Each batch of the tile's sorted list is gathered once into
 // shared memory and compacted to the Gaussians whose conservative skip box
-// meets the tile; all threads then read the records as broadcasts.  A CTA
-// leaves the list as soon as every pixel has saturated (__syncthreads_and on
-// the per-pixel stop flag), which changes no pixel: a stopped pixel takes no
-// further Gaussian in the reference either.
+// meets the tile; their SH rows arrive by cp.async.bulk (the TMA engine) on
+// an mbarrier; all threads then read the records as broadcasts.  Each warp
+// walks only the batch Gaussians whose skip box and skip ellipse meet its
+// pixel block.  A CTA leaves the list as soon as every pixel has saturated
+// (__syncthreads_and on the per-pixel stop flag), which changes no pixel: a
+// stopped pixel takes no further Gaussian in the reference either.
 //
 // Arithmetic.  Everything that decides which pairs contribute -- the radial
 // distance, the exponential G (gsx_expf), a*G < 1/255, the transmittance T --

@@ -440,7 +440,6 @@ def _zeroed_grad_buffers(device, n: int, sh: torch.Tensor):
     return bufs, done
 
 
-
 def _copy_stream(device) -> torch.cuda.Stream:
     key = (device.type, device.index)
     if key not in _copy_streams:
