@@ -31,7 +31,12 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kItems = 16;
-constexpr int kTile = kThreads * kItems;  // keys per chunk
+constexpr int kTile = kThreads * kItems;  // keys per chunk (8-bit digits)
+// 9-bit digits (two passes for 17-18-bit tile ids, e.g. a batch of views
+// with up to 2^18 tiles): 512 buckets, 12 keys per thread to stay within
+// 48 KB of static shared memory
+constexpr int kItems9 = 12;
+constexpr int kTileMin = kThreads * kItems9;  // smallest chunk: sizes the look-back rows
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kCountMask = (1u << 30) - 1u;
@@ -92,28 +97,33 @@ __device__ __forceinline__ T block_exclusive_scan(T v, T *s_tmp, T *total) {
   return x - v + wsum;
 }
 
-// Histogram of `passes` 8-bit digits (starting at bit 0) of n keys.
+// Histogram of `passes` RB-bit digits (starting at bit 0) of n keys.
+template <int RB>
 __global__ void __launch_bounds__(kThreads)
     histogram_kernel(const uint32_t *__restrict__ keys, uint32_t n_max,
                      const uint32_t *__restrict__ n_dev, int passes,
                      uint32_t *__restrict__ hist) {
-  __shared__ uint32_t sh[4 * 256];
+  constexpr uint32_t RADIX = 1u << RB, MASK = RADIX - 1u;
+  __shared__ uint32_t sh[4 * 256];  // passes * RADIX <= 1024
   const uint32_t n = n_dev ? min(*n_dev, n_max) : n_max;
   for (int i = threadIdx.x; i < 4 * 256; i += kThreads) sh[i] = 0;
   __syncthreads();
   for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
     const uint32_t k = keys[i];
-    for (int p = 0; p < passes; ++p) atomicAdd(&sh[p * 256 + ((k >> (8 * p)) & 255u)], 1u);
+    for (int p = 0; p < passes; ++p) atomicAdd(&sh[p * RADIX + ((k >> (RB * p)) & MASK)], 1u);
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < passes * 256; i += kThreads)
+  for (int i = threadIdx.x; i < passes * (int)RADIX; i += kThreads)
     if (sh[i]) atomicAdd(&hist[i], sh[i]);
 }
 
-// One stable LSD pass on the 8-bit digit at `shift`.  vals_in == nullptr
-// means value = input position.  The item count is n_max, or *n_dev when
-// given (a count produced on the device); chunks past it exit at once, and
-// no chunk ever waits on a later one.
+// One stable LSD pass on the RB-bit digit at `shift` (RB = 8 or 9), chunks
+// of kThreads * ITEMS keys; thread t owns digits t*DPT .. t*DPT + DPT - 1.
+// vals_in == nullptr means value = input position.  The item count is n_max,
+// or *n_dev when given (a count produced on the device); chunks past it exit
+// at once, and no chunk ever waits on a later one.  `status` holds RADIX
+// look-back words per chunk.
+template <int RB, int ITEMS>
 __global__ void __launch_bounds__(kThreads)
     onesweep_kernel(const uint32_t *__restrict__ keys_in,
                     const uint32_t *__restrict__ vals_in, uint32_t *__restrict__ keys_out,
@@ -121,34 +131,38 @@ __global__ void __launch_bounds__(kThreads)
                     const uint32_t *__restrict__ n_dev, int shift,
                     const uint32_t *__restrict__ pass_hist, uint32_t *status,
                     uint32_t *chunk_counter, uint32_t *error) {
+  constexpr uint32_t RADIX = 1u << RB, MASK = RADIX - 1u;
+  constexpr int DPT = (int)RADIX / kThreads;  // digits per thread
+  constexpr int TILE = kThreads * ITEMS;
+  static_assert(DPT >= 1 && DPT * kThreads == (int)RADIX, "RADIX must be a multiple of kThreads");
   const uint32_t n = n_dev ? min(*n_dev, n_max) : n_max;
-  __shared__ uint32_t s_warp[kWarps][256];
-  __shared__ uint32_t s_cta_excl[256];
-  __shared__ uint32_t s_glob[256];
+  __shared__ uint32_t s_warp[kWarps][RADIX];
+  __shared__ uint32_t s_cta_excl[RADIX];
+  __shared__ uint32_t s_glob[RADIX];
   __shared__ uint32_t s_tmp[kWarps];
-  __shared__ uint32_t s_keys[kTile];
-  __shared__ uint32_t s_vals[kTile];
+  __shared__ uint32_t s_keys[TILE];
+  __shared__ uint32_t s_vals[TILE];
   __shared__ uint32_t s_chunk;
 
   const int t = threadIdx.x, w = t >> 5, lane = t & 31;
   if (t == 0) s_chunk = atomicAdd(chunk_counter, 1u);
-  for (int i = t; i < kWarps * 256; i += kThreads) (&s_warp[0][0])[i] = 0;
+  for (int i = t; i < kWarps * (int)RADIX; i += kThreads) (&s_warp[0][0])[i] = 0;
   __syncthreads();
   const uint32_t chunk = s_chunk;
-  const uint32_t base = chunk * (uint32_t)kTile;
+  const uint32_t base = chunk * (uint32_t)TILE;
   if (base >= n) return;  // block-uniform
   const uint32_t lt = lanemask_lt();
 
-  uint32_t keys[kItems], vals[kItems], rank[kItems];
+  uint32_t keys[ITEMS], vals[ITEMS], rank[ITEMS];
 #pragma unroll
-  for (int j = 0; j < kItems; ++j) {
-    const uint32_t idx = base + w * (32 * kItems) + j * 32 + lane;
+  for (int j = 0; j < ITEMS; ++j) {
+    const uint32_t idx = base + w * (32 * ITEMS) + j * 32 + lane;
     const bool valid = idx < n;
     const uint32_t k = valid ? keys_in[idx] : 0u;
     keys[j] = k;
     vals[j] = valid ? (vals_in ? vals_in[idx] : idx) : 0u;
-    const uint32_t d = (k >> shift) & 255u;
-    const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 256u);
+    const uint32_t d = (k >> shift) & MASK;
+    const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : RADIX);
     uint32_t cnt = 0;
     if (valid) cnt = s_warp[w][d];
     __syncwarp();
@@ -159,62 +173,85 @@ __global__ void __launch_bounds__(kThreads)
   }
   __syncthreads();
 
-  // per digit (thread t = digit t): exclusive prefix over warps, CTA total
-  uint32_t total = 0;
+  // per digit: exclusive prefix over warps, CTA total
+  uint32_t total[DPT], hsum[DPT];
+  uint32_t tsum = 0, hs = 0;
 #pragma unroll
-  for (int ww = 0; ww < kWarps; ++ww) {
-    const uint32_t c = s_warp[ww][t];
-    s_warp[ww][t] = total;
-    total += c;
-  }
-  const uint32_t cta_excl = block_exclusive_scan<uint32_t>(total, s_tmp, nullptr);
-  s_cta_excl[t] = cta_excl;
-  const uint32_t gbase = block_exclusive_scan<uint32_t>(pass_hist[t], s_tmp, nullptr);
-
-  // decoupled look-back for digit t
-  uint32_t prev = 0;
-  uint32_t *mine = status + (size_t)chunk * 256 + t;
-  if (chunk == 0) {
-    st_volatile(mine, kFlagPrefix | total);
-  } else {
-    st_volatile(mine, kFlagAgg | total);
-    int64_t c = (int64_t)chunk - 1;
-    uint32_t spins = 0;
-    while (c >= 0) {
-      const uint32_t sv = ld_volatile(status + (size_t)c * 256 + t);
-      const uint32_t flag = sv & ~kCountMask;
-      if (flag == 0u) {
-        if (++spins > kSpinLimit) {
-          atomicOr(error, kErrTimeout);
-          break;
-        }
-        __nanosleep(32);
-        continue;
-      }
-      prev += sv & kCountMask;
-      if (flag == kFlagPrefix) break;
-      --c;
+  for (int q = 0; q < DPT; ++q) {
+    const int d = t * DPT + q;
+    uint32_t run = 0;
+#pragma unroll
+    for (int ww = 0; ww < kWarps; ++ww) {
+      const uint32_t c = s_warp[ww][d];
+      s_warp[ww][d] = run;
+      run += c;
     }
-    st_volatile(mine, kFlagPrefix | (prev + total));
+    total[q] = run;
+    tsum += run;
+    hsum[q] = pass_hist[d];
+    hs += hsum[q];
   }
-  s_glob[t] = gbase + prev;
+  uint32_t cta_excl = block_exclusive_scan<uint32_t>(tsum, s_tmp, nullptr);
+  uint32_t gbase = block_exclusive_scan<uint32_t>(hs, s_tmp, nullptr);
+
+  // decoupled look-back for this thread's digits: publish every aggregate
+  // first, then walk back
+  uint32_t prev[DPT];
+#pragma unroll
+  for (int q = 0; q < DPT; ++q) {
+    prev[q] = 0;
+    uint32_t *mine = status + (size_t)chunk * RADIX + t * DPT + q;
+    st_volatile(mine, (chunk == 0 ? kFlagPrefix : kFlagAgg) | total[q]);
+  }
+  if (chunk > 0) {
+#pragma unroll
+    for (int q = 0; q < DPT; ++q) {
+      const int d = t * DPT + q;
+      int64_t c = (int64_t)chunk - 1;
+      uint32_t spins = 0;
+      while (c >= 0) {
+        const uint32_t sv = ld_volatile(status + (size_t)c * RADIX + d);
+        const uint32_t flag = sv & ~kCountMask;
+        if (flag == 0u) {
+          if (++spins > kSpinLimit) {
+            atomicOr(error, kErrTimeout);
+            break;
+          }
+          __nanosleep(32);
+          continue;
+        }
+        prev[q] += sv & kCountMask;
+        if (flag == kFlagPrefix) break;
+        --c;
+      }
+      st_volatile(status + (size_t)chunk * RADIX + d, kFlagPrefix | (prev[q] + total[q]));
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < DPT; ++q) {
+    const int d = t * DPT + q;
+    s_cta_excl[d] = cta_excl;
+    s_glob[d] = gbase + prev[q];
+    cta_excl += total[q];
+    gbase += hsum[q];
+  }
   __syncthreads();
 
 #pragma unroll
-  for (int j = 0; j < kItems; ++j) {
-    const uint32_t idx = base + w * (32 * kItems) + j * 32 + lane;
+  for (int j = 0; j < ITEMS; ++j) {
+    const uint32_t idx = base + w * (32 * ITEMS) + j * 32 + lane;
     if (idx < n) {
-      const uint32_t d = (keys[j] >> shift) & 255u;
+      const uint32_t d = (keys[j] >> shift) & MASK;
       const uint32_t pos = s_cta_excl[d] + s_warp[w][d] + rank[j];
       s_keys[pos] = keys[j];
       s_vals[pos] = vals[j];
     }
   }
   __syncthreads();
-  const uint32_t cnt = min((uint32_t)kTile, n - base);
+  const uint32_t cnt = min((uint32_t)TILE, n - base);
   for (uint32_t i = t; i < cnt; i += kThreads) {
     const uint32_t k = s_keys[i];
-    const uint32_t d = (k >> shift) & 255u;
+    const uint32_t d = (k >> shift) & MASK;
     const uint32_t gpos = s_glob[d] + (i - s_cta_excl[d]);
     if (gpos < n) {  // always true unless a look-back wait expired
       keys_out[gpos] = k;
@@ -507,32 +544,44 @@ Workspace carve_ws(void *base, int64_t n, int64_t cap) {
   w.emit_status = reinterpret_cast<unsigned long long *>(take(8 * w.emit_words));
   w.depth_chunks = (nn + kTile - 1) / kTile;
   w.status_depth = reinterpret_cast<uint32_t *>(take(4 * 256 * kMaxPasses * w.depth_chunks));
-  w.tile_chunks = (cc + kTile - 1) / kTile;
+  w.tile_chunks = (cc + kTileMin - 1) / kTileMin;
   w.status_tile = reinterpret_cast<uint32_t *>(take(4 * 256 * kMaxPasses * w.tile_chunks));
   w.bytes = off;
   return w;
 }
 
+// Digit width and pass count of an LSD sort over `bits` key bits: 8-bit
+// digits, except that 17-18 bits take two 9-bit passes instead of three.
+inline int digit_bits(int bits) { return (bits == 17 || bits == 18) ? 9 : 8; }
+inline int sort_passes(int bits) { return (bits + digit_bits(bits) - 1) / digit_bits(bits); }
+
 // Stable LSD sort of n (key, value) pairs over `bits` low key bits; the count
 // is n_max, or *n_dev (at most n_max) when n_dev is given.  The final pass
 // writes into (final_keys, final_vals); intermediate passes use the two
-// scratch buffers.  keys_in/vals_in are never written.  `hist` (4 x 256
-// digit counts), `tickets` (4 chunk counters) and `status` (4 passes of
-// `chunks_cap` look-back rows) must be zero on entry.
+// scratch buffers.  keys_in/vals_in are never written.  `hist` (up to 1024
+// digit counts), `tickets` (one chunk counter per pass) and `status` (per
+// pass, `chunks_cap` rows of 2^digit_bits look-back words) must be zero on
+// entry.
 int radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t n_max,
                const uint32_t *n_dev, int bits, uint32_t *scratch_k[2], uint32_t *scratch_v[2],
                uint32_t *final_keys, uint32_t *final_vals, uint32_t *hist, uint32_t *tickets,
                uint32_t *status, size_t chunks_cap, uint32_t *error, cudaStream_t s) {
-  const int passes = (bits + 7) / 8;
-  if (n_max == 0 || passes == 0) return GSX_OK;
+  const int rb = digit_bits(bits), passes = sort_passes(bits);
+  if (n_max == 0 || bits == 0) return GSX_OK;
+  const uint32_t radix = 1u << rb;
   uint32_t hist_grid = (n_max + kThreads * 16 - 1) / (kThreads * 16);
   if (hist_grid > 1024u) hist_grid = 1024u;
   count_launches(1);
-  histogram_kernel<<<hist_grid, kThreads, 0, s>>>(keys_in, n_max, n_dev, passes, hist);
+  if (rb == 9)
+    histogram_kernel<9><<<hist_grid, kThreads, 0, s>>>(keys_in, n_max, n_dev, passes, hist);
+  else
+    histogram_kernel<8><<<hist_grid, kThreads, 0, s>>>(keys_in, n_max, n_dev, passes, hist);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_status(e, "histogram_kernel launch");
-  const uint32_t chunks = (n_max + kTile - 1) / kTile;
-  if (chunks > chunks_cap) {
+  const uint32_t tile = kThreads * (rb == 9 ? kItems9 : kItems);
+  const uint32_t chunks = (n_max + tile - 1) / tile;
+  // rows are laid out for 256-word digits: a 512-word pass takes two rows' room
+  if ((size_t)chunks * radix * passes > chunks_cap * 256 * 4) {
     set_error("radix sort of %u keys needs %u chunks, the workspace holds %zu", n_max, chunks,
               chunks_cap);
     return GSX_ERR_CAPACITY;
@@ -542,10 +591,14 @@ int radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t n_max,
     const bool last = p == passes - 1;
     uint32_t *ko = last ? final_keys : scratch_k[p & 1];
     uint32_t *vo = last ? final_vals : scratch_v[p & 1];
+    uint32_t *st = status + (size_t)chunks * radix * p;
     count_launches(1);
-    onesweep_kernel<<<chunks, kThreads, 0, s>>>(ki, vi, ko, vo, n_max, n_dev, 8 * p,
-                                                 hist + 256 * p, status + chunks_cap * 256 * p,
-                                                 tickets + p, error);
+    if (rb == 9)
+      onesweep_kernel<9, kItems9><<<chunks, kThreads, 0, s>>>(
+          ki, vi, ko, vo, n_max, n_dev, rb * p, hist + radix * p, st, tickets + p, error);
+    else
+      onesweep_kernel<8, kItems><<<chunks, kThreads, 0, s>>>(
+          ki, vi, ko, vo, n_max, n_dev, rb * p, hist + radix * p, st, tickets + p, error);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e, "onesweep_kernel launch");
     ki = ko;
@@ -586,10 +639,13 @@ int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
     return GSX_ERR_INVALID_ARG;
   }
   const int tile_bits = bits_for((uint64_t)(n_tiles > 0 ? n_tiles - 1 : 0));
-  const int tile_passes = (tile_bits + 7) / 8;
-  // one clear of the zero-initialised state, through the last tile pass in use
+  const int tile_passes = tile_bits == 0 ? 0 : sort_passes(tile_bits);
+  // one clear of the zero-initialised state, through the last tile pass in
+  // use (a pass's rows are packed: chunks x 2^digit_bits words)
+  const uint32_t tile_chunk_keys = kThreads * (digit_bits(tile_bits) == 9 ? kItems9 : kItems);
+  const size_t tile_rows = ((size_t)(capacity > 0 ? capacity : 1) + tile_chunk_keys - 1) / tile_chunk_keys;
   const char *zero_end = reinterpret_cast<const char *>(w.status_tile) +
-                         (size_t)4 * 256 * tile_passes * w.tile_chunks;
+                         (size_t)4 * tile_rows * ((size_t)1 << digit_bits(tile_bits)) * tile_passes;
   cudaError_t e = cudaMemsetAsync(start, 0xff, sizeof(int32_t) * (size_t)n_tiles, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(end, 0xff, sizeof(int32_t) * (size_t)n_tiles, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(w.zero_begin, 0, (size_t)(zero_end - w.zero_begin), s);
@@ -624,7 +680,7 @@ int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
     e = cudaMemcpyAsync(ids_u, w.tvals[0], 4 * (size_t)cap, cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return cuda_status(e, "copy ids");
   } else {
-    const int passes = (tile_bits + 7) / 8;
+    const int passes = sort_passes(tile_bits);
     uint32_t *tk[2] = {w.tkeys[1], w.tkeys[0]}, *tv[2] = {w.tvals[1], w.tvals[0]};
     final_keys = (passes & 1) ? w.tkeys[1] : w.tkeys[0];
     st = radix_sort(w.tkeys[0], w.tvals[0], cap, w.k_eff, tile_bits, tk, tv, final_keys, ids_u,

@@ -117,3 +117,23 @@ def test_autotuner_picks_a_listed_shape():
     best, times = B.autotune_tile([scene_t], views, reps=1, device=dev())
     assert best in times and set(times) == {(8, 8), (16, 16), (32, 8)}
     assert all(t > 0 for t in times.values())
+
+
+def test_batch_with_more_than_65536_tiles_matches_per_view():
+    """9 views of 1920x1080 at 16x16 tiles: 73,440 tiles, so the batched tile
+    ids take 17 bits and the tile sort runs two 9-bit passes; every image
+    must still equal the view rendered alone."""
+    sc = S.custom_workload(3000, 64, 64, 3, seed=37).scene
+    scene_t = B.Scene.from_arrays(sc, dev())
+    views = make_views(9, seed=37, sizes=((1920, 1080),))
+    st = renderer.RasterSettings()
+    total_tiles = sum(((c.w + 15) // 16) * ((c.h + 15) // 16) for _, c in views)
+    assert 1 << 16 < total_tiles <= 1 << 18
+    bp = B.BatchPipeline(dev(), st).plan([scene_t], [B.ViewSpec(0, c, cam) for c, cam in views],
+                                         backward=False)
+    bp.forward()
+    torch.cuda.synchronize()
+    params = [scene_t.mean, scene_t.qvec, scene_t.log_scale, scene_t.sh, scene_t.alpha_logit]
+    for i, (c2w, cam) in enumerate(views):
+        img = renderer.rasterize(*params, c2w, cam, st)
+        np.testing.assert_array_equal(bp.images[i].cpu().numpy(), img.cpu().numpy())

@@ -333,3 +333,23 @@ def test_thin_rotated_gaussians_match_oracle():
     assert_image_close(got["image"], ref["image"])
     for k, g in got["grads"].items():
         assert rel_err(g, ref["param_grads"][k]) <= GRAD_REL, k
+
+
+def test_17_bit_tile_ids_bitexact():
+    """3840x2160 with 8x8 tiles has 129,600 tiles: the tile sort runs two
+    9-bit passes; lists and image must match the oracle exactly."""
+    wl = S.custom_workload(3000, 3840, 2160, 1, seed=41, tile=8)
+    view = wl.views[0]
+    assert 1 << 16 < (3840 // 8) * (2160 // 8) <= 1 << 18
+    ref = oracle_view(wl)
+    st = renderer.RasterSettings(tile_w=8, tile_h=8)
+    pr = ref["proj"]
+    proj = renderer.Projected(t(pr["mean2d"]), t(pr["cov2d"]), t(pr["depth"]), t(pr["alpha"]),
+                              t(pr["rect"], torch.int32), t(pr["counts"], torch.int32))
+    ids, start, end, K = renderer.bin_gaussians(proj, 3840 // 8, 2160 // 8)
+    assert K == ref["bins"]["K"]
+    np.testing.assert_array_equal(ids.cpu().numpy(), ref["bins"]["ids"])
+    np.testing.assert_array_equal(start.cpu().numpy(), ref["bins"]["start"])
+    np.testing.assert_array_equal(end.cpu().numpy(), ref["bins"]["end"])
+    got = gpu_pipeline(wl, st, with_grad=False)
+    assert_image_close(got["image"], ref["image"])
