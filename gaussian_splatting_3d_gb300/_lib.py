@@ -115,9 +115,18 @@ SIGNATURES = {
         c_int,
         [POINTER(GsxRasterParams), c_int64, c_int64, P, P, P, P, P, P, P, P, P, P, P],
     ),
+    "gsx_tile_order": (c_int, [P, P, c_int32, P, P]),
+    "gsx_render_forward_ordered": (
+        c_int,
+        [POINTER(GsxRasterParams), c_int64, c_int64, P, P, P, P, P, P, P, P, P, P, P, P],
+    ),
     "gsx_render_forward_maps": (
         c_int,
         [POINTER(GsxRasterParams), c_int64, c_int64, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P],
+    ),
+    "gsx_render_backward_ordered": (
+        c_int,
+        [POINTER(GsxRasterParams), c_int64, c_int64] + [P] * 17,
     ),
     "gsx_render_backward": (
         c_int,

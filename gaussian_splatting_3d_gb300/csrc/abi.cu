@@ -304,12 +304,12 @@ int gsx_project_forward(int64_t n, const float *mean, const float *qvec,
                                 cov2d, depth, alpha, rect, counts, as_stream(stream));
 }
 
-int gsx_render_forward_maps(const gsx_raster_params *p, int64_t n, int64_t n_keys,
-                            const float *mean2d, const float *cov2d, const float *sh,
-                            const float *alpha, const int32_t *start, const int32_t *end,
-                            const int32_t *gaussian_ids, const float *topleft, const float *c2w,
-                            float *out, const float *bg_rgb, const float *depth,
-                            float *alpha_out, float *depth_out, void *stream) {
+static int render_forward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
+                          const float *mean2d, const float *cov2d, const float *sh,
+                          const float *alpha, const int32_t *start, const int32_t *end,
+                          const int32_t *gaussian_ids, const float *topleft, const float *c2w,
+                          float *out, const float *bg_rgb, const float *depth, float *alpha_out,
+                          float *depth_out, const int32_t *tile_order, void *stream) {
   g_err[0] = 0;
   GSX_REQUIRE(p, "null params");
   RasterArgs a = make_args(p->tile_w, p->tile_h, (uint32_t)p->n_tiles_w,
@@ -339,9 +339,44 @@ int gsx_render_forward_maps(const gsx_raster_params *p, int64_t n, int64_t n_key
   a.depth = depth;
   a.alpha_out = alpha_out;
   a.depth_out = depth_out;
+  a.tile_order = tile_order;
   int st = check_raster(a, p->sh_order, n, n_keys);
   if (st != GSX_OK) return st;
   return launch_raster_forward(a, p->sh_order, as_stream(stream));
+}
+
+int gsx_render_forward_maps(const gsx_raster_params *p, int64_t n, int64_t n_keys,
+                            const float *mean2d, const float *cov2d, const float *sh,
+                            const float *alpha, const int32_t *start, const int32_t *end,
+                            const int32_t *gaussian_ids, const float *topleft, const float *c2w,
+                            float *out, const float *bg_rgb, const float *depth,
+                            float *alpha_out, float *depth_out, void *stream) {
+  return render_forward(p, n, n_keys, mean2d, cov2d, sh, alpha, start, end, gaussian_ids, topleft,
+                        c2w, out, bg_rgb, depth, alpha_out, depth_out, nullptr, stream);
+}
+
+int gsx_render_forward_ordered(const gsx_raster_params *p, int64_t n, int64_t n_keys,
+                               const float *mean2d, const float *cov2d, const float *sh,
+                               const float *alpha, const int32_t *start, const int32_t *end,
+                               const int32_t *gaussian_ids, const float *topleft,
+                               const float *c2w, float *out, const int32_t *tile_order,
+                               void *stream) {
+  if (!tile_order) {
+    g_err[0] = 0;
+    set_error("null tile_order");
+    return GSX_ERR_INVALID_ARG;
+  }
+  return render_forward(p, n, n_keys, mean2d, cov2d, sh, alpha, start, end, gaussian_ids, topleft,
+                        c2w, out, nullptr, nullptr, nullptr, nullptr, tile_order, stream);
+}
+
+int gsx_tile_order(const int32_t *start, const int32_t *end, int32_t n_tiles, int32_t *tile_order,
+                   void *stream) {
+  g_err[0] = 0;
+  GSX_REQUIRE(n_tiles >= 0, "n_tiles must be >= 0 (got %d)", n_tiles);
+  if (n_tiles == 0) return GSX_OK;
+  GSX_REQUIRE(start && end && tile_order, "null pointer argument");
+  return launch_tile_order(start, end, n_tiles, tile_order, as_stream(stream));
 }
 
 int gsx_render_forward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
@@ -353,14 +388,13 @@ int gsx_render_forward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
                                  topleft, c2w, out, nullptr, nullptr, nullptr, nullptr, stream);
 }
 
-int gsx_render_backward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
-                        const float *mean2d, const float *cov2d, const float *sh,
-                        const float *alpha, const int32_t *start,
-                        const int32_t *end, const int32_t *gaussian_ids,
-                        const float *topleft, const float *c2w, const float *out,
-                        const float *grad_out, float *grad_mean2d,
-                        float *grad_cov2d, float *grad_sh, float *grad_alpha,
-                        void *stream) {
+static int render_backward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
+                           const float *mean2d, const float *cov2d, const float *sh,
+                           const float *alpha, const int32_t *start, const int32_t *end,
+                           const int32_t *gaussian_ids, const float *topleft, const float *c2w,
+                           const float *out, const float *grad_out, float *grad_mean2d,
+                           float *grad_cov2d, float *grad_sh, float *grad_alpha,
+                           const int32_t *tile_order, void *stream) {
   g_err[0] = 0;
   GSX_REQUIRE(p, "null params");
   RasterArgs a = make_args(p->tile_w, p->tile_h, (uint32_t)p->n_tiles_w,
@@ -389,7 +423,38 @@ int gsx_render_backward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
   if (st != GSX_OK) return st;
   GSX_REQUIRE(grad_out && (n == 0 || (grad_mean2d && grad_cov2d && grad_sh && grad_alpha)),
               "null gradient pointer");
+  a.tile_order = tile_order;
   return launch_raster_backward(a, p->sh_order, as_stream(stream));
+}
+
+int gsx_render_backward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
+                        const float *mean2d, const float *cov2d, const float *sh,
+                        const float *alpha, const int32_t *start,
+                        const int32_t *end, const int32_t *gaussian_ids,
+                        const float *topleft, const float *c2w, const float *out,
+                        const float *grad_out, float *grad_mean2d,
+                        float *grad_cov2d, float *grad_sh, float *grad_alpha,
+                        void *stream) {
+  return render_backward(p, n, n_keys, mean2d, cov2d, sh, alpha, start, end, gaussian_ids,
+                         topleft, c2w, out, grad_out, grad_mean2d, grad_cov2d, grad_sh,
+                         grad_alpha, nullptr, stream);
+}
+
+int gsx_render_backward_ordered(const gsx_raster_params *p, int64_t n, int64_t n_keys,
+                                const float *mean2d, const float *cov2d, const float *sh,
+                                const float *alpha, const int32_t *start, const int32_t *end,
+                                const int32_t *gaussian_ids, const float *topleft,
+                                const float *c2w, const float *out, const float *grad_out,
+                                float *grad_mean2d, float *grad_cov2d, float *grad_sh,
+                                float *grad_alpha, const int32_t *tile_order, void *stream) {
+  if (!tile_order) {
+    g_err[0] = 0;
+    set_error("null tile_order");
+    return GSX_ERR_INVALID_ARG;
+  }
+  return render_backward(p, n, n_keys, mean2d, cov2d, sh, alpha, start, end, gaussian_ids,
+                         topleft, c2w, out, grad_out, grad_mean2d, grad_cov2d, grad_sh,
+                         grad_alpha, tile_order, stream);
 }
 
 int gsx_raster_status(uint32_t *flags, int32_t clear, void *stream) {

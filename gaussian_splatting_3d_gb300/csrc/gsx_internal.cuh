@@ -140,8 +140,15 @@ struct RasterArgs {
   float bg[3];
   const float *depth;  // per-item camera depth (needed for depth_out)
   float *alpha_out, *depth_out;
+  // single view: CTA b renders tile tile_order[b] (a permutation of the tiles,
+  // longest lists first); nullptr renders tile b
+  const int32_t *tile_order;
 };
 int launch_raster_forward(const RasterArgs &a, int C, cudaStream_t s);
+// order[0..n_tiles) = the tiles by descending list length (end - start), in
+// log-spaced length classes; the order within a class is unspecified.
+int launch_tile_order(const int32_t *start, const int32_t *end, int32_t n_tiles, int32_t *order,
+                      cudaStream_t s);
 int launch_raster_backward(const RasterArgs &a, int C, cudaStream_t s);
 // Batched: a.views/a.n_views set, grid = total tiles (all views share the tile
 // shape and SH order; the per-view fields of `a` are ignored).

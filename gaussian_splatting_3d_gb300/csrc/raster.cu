@@ -163,7 +163,11 @@ __device__ __forceinline__ ViewCtx make_ctx(const RasterArgs &a) {
   ViewCtx c;
   c.gtile = blockIdx.x;
   if constexpr (!BATCHED) {
-    c.tile = blockIdx.x;
+    if (a.tile_order) {  // an entry outside the grid renders nothing (gtile = -1)
+      const int g = a.tile_order[blockIdx.x];
+      c.gtile = (g >= 0 && g < (int)gridDim.x) ? g : -1;
+    }
+    c.tile = c.gtile;
     c.n_tiles_w = a.n_tiles_w;
     c.tile_w = a.tile_w;
     c.tile_h = a.tile_h;
@@ -567,6 +571,7 @@ __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a
   int *wl = reinterpret_cast<int *>(L.sh + B * GSH) + (threadIdx.x >> 5) * B;  // [nwarps][B]
 
   const ViewCtx ctx = make_ctx<BATCHED>(a);
+  if (ctx.gtile < 0) return;  // CTA-uniform: not a tile of the grid
   const int t = threadIdx.x, lane = t & 31;
   int gx, gy;
   pixel_of(ctx, t, gx, gy);
@@ -803,6 +808,7 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
   int *wl = s_touched + B + (threadIdx.x >> 5) * B;                       // [nwarps][B]
 
   const ViewCtx ctx = make_ctx<BATCHED>(a);
+  if (ctx.gtile < 0) return;  // CTA-uniform: not a tile of the grid
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   int gx, gy;
   pixel_of(ctx, t, gx, gy);
@@ -1086,6 +1092,104 @@ int dispatch_bwd(const RasterArgs &a, int C, int64_t grid, cudaStream_t s) {
 }
 
 }  // namespace
+
+// Longest-processing-time-first order of the tiles for the raster passes:
+// their grids run in ~13-18 waves of CTAs, and the tail is set by the heavy
+// tiles (long lists) when they start late.  One CTA: a histogram of 256
+// log-spaced length classes (8 per doubling), its exclusive scan from the
+// longest class down, then each tile claims a slot in its class (lanes of a
+// warp with the same class claim together).  Classes of the first
+// kOrderCache tiles per thread stay in registers between the two passes.
+constexpr int kOrderThreads = 1024, kOrderCache = 16;
+
+__device__ __forceinline__ uint32_t length_class(const int32_t *__restrict__ start,
+                                                 const int32_t *__restrict__ end, int tile) {
+  const int32_t s0 = start[tile], e0 = end[tile];
+  const uint32_t len = (s0 >= 0 && e0 > s0) ? (uint32_t)(e0 - s0) : 0u;
+  // 8 classes per doubling of len + 1 (log2 with 3 mantissa bits); longest = class 0
+  const uint32_t v = len + 1u;
+  const int e = 31 - __clz(v);
+  const uint32_t frac = e >= 3 ? (v >> (e - 3)) & 7u : (v << (3 - e)) & 7u;
+  return 255u - ((uint32_t)e * 8u + frac);
+}
+
+__global__ void __launch_bounds__(kOrderThreads) tile_order_kernel(const int32_t *__restrict__ start,
+                                                                   const int32_t *__restrict__ end,
+                                                                   int32_t n_tiles,
+                                                                   int32_t *__restrict__ order) {
+  __shared__ uint32_t s_cnt[256];
+  const int t = threadIdx.x, lane = t & 31;
+  if (t < 256) s_cnt[t] = 0;
+  __syncthreads();
+  uint32_t cache[kOrderCache];
+  const int rounds = (n_tiles + kOrderThreads - 1) / kOrderThreads;  // CTA-uniform
+  // all cached rounds' loads first, so their latencies overlap
+#pragma unroll
+  for (int k = 0; k < kOrderCache; ++k) {
+    const int i = k * kOrderThreads + t;
+    cache[k] = i < n_tiles ? length_class(start, end, i) : 256u;
+  }
+  for (int k = 0; k < rounds; ++k) {
+    const int i = k * kOrderThreads + t;
+    uint32_t c = 256u;
+    if (k < kOrderCache) {
+#pragma unroll
+      for (int q = 0; q < kOrderCache; ++q)
+        if (q == k) c = cache[q];
+    } else if (i < n_tiles) {
+      c = length_class(start, end, i);
+    }
+    const uint32_t peers = __match_any_sync(0xffffffffu, c);
+    if (c < 256u && (peers & ((1u << lane) - 1u)) == 0) atomicAdd(&s_cnt[c], __popc(peers));
+  }
+  __syncthreads();
+  if (t < 32) {  // exclusive scan of the 256 class counts, 8 per lane
+    uint32_t v[8], sum = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      v[q] = s_cnt[8 * t + q];
+      sum += v[q];
+    }
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (t >= o) incl += y;
+    }
+    uint32_t run = incl - sum;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      s_cnt[8 * t + q] = run;
+      run += v[q];
+    }
+  }
+  __syncthreads();
+  for (int k = 0; k < rounds; ++k) {
+    const int i = k * kOrderThreads + t;
+    uint32_t c = 256u;
+    if (k < kOrderCache) {
+#pragma unroll
+      for (int q = 0; q < kOrderCache; ++q)
+        if (q == k) c = cache[q];
+    } else if (i < n_tiles) {
+      c = length_class(start, end, i);
+    }
+    const uint32_t peers = __match_any_sync(0xffffffffu, c);
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (c < 256u && lane == leader) base = atomicAdd(&s_cnt[c], __popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (c < 256u) order[base + __popc(peers & ((1u << lane) - 1u))] = i;
+  }
+}
+
+int launch_tile_order(const int32_t *start, const int32_t *end, int32_t n_tiles, int32_t *order,
+                      cudaStream_t s) {
+  if (n_tiles <= 0) return GSX_OK;
+  count_launches(1);
+  tile_order_kernel<<<1, kOrderThreads, 0, s>>>(start, end, n_tiles, order);
+  return cuda_status(cudaGetLastError(), "tile_order_kernel launch");
+}
 
 int launch_raster_forward(const RasterArgs &a, int C, cudaStream_t s) {
   const int64_t grid = (int64_t)a.n_tiles_w * a.n_tiles_h;

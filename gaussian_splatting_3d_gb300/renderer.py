@@ -276,22 +276,26 @@ class ViewPipeline:
             cam_consts = camera_consts(c2w_np, cam).to(dev, non_blocking=True)
         topleft, c2w_dev = cam_consts[:2], cam_consts[2:]
         out = torch.empty((cam.h, cam.w, 3), dtype=torch.float32, device=dev)
+        order = torch.empty((ntw * nth,), dtype=torch.int32, device=dev)
         params = _raster_params(cam, settings, C, sh_stride)
         grads = grads_ready = None
         cap = max(self.key_capacity, 1 << 16)
+        want_grads = prepare_grads and not settings.recompute_projection
         for _ in range(3):
             with ev("binning"):
                 ids, start, end = bin_gaussians_async(pr, ntw, nth, cap)
-            if prepare_grads and grads is None and not settings.recompute_projection:
-                # after the binning (whose working set lives in L2), beside the raster
-                grads, grads_ready = _zeroed_grad_buffers(dev, n, sh)
+            if want_grads and grads is None:
+                binned = torch.cuda.Event()
+                binned.record(torch.cuda.current_stream(dev))
             if sh_ready is not None:  # only the raster reads the SH coefficients
                 torch.cuda.current_stream(dev).wait_event(sh_ready)
             with ev("raster_fwd"):
                 if settings.bg is None and not settings.output_maps:
-                    _lib.call("gsx_render_forward", ctypes.byref(params), n, cap, ptr(pr.mean2d), ptr(pr.cov2d),
-                              ptr(sh), ptr(pr.alpha), ptr(start), ptr(end), ptr(ids), ptr(topleft), ptr(c2w_dev),
-                              ptr(out), stream_handle(dev))
+                    # longest tile lists first: the order changes the schedule, not the image
+                    _lib.call("gsx_tile_order", ptr(start), ptr(end), ntw * nth, ptr(order), stream_handle(dev))
+                    _lib.call("gsx_render_forward_ordered", ctypes.byref(params), n, cap, ptr(pr.mean2d),
+                              ptr(pr.cov2d), ptr(sh), ptr(pr.alpha), ptr(start), ptr(end), ptr(ids), ptr(topleft),
+                              ptr(c2w_dev), ptr(out), ptr(order), stream_handle(dev))
                 else:
                     bg = (ctypes.c_float * 3)(*settings.bg) if settings.bg is not None else None
                     if settings.output_maps:
@@ -302,6 +306,10 @@ class ViewPipeline:
                               ptr(c2w_dev), ptr(out), ctypes.addressof(bg) if bg is not None else None,
                               ptr(pr.depth), ptr(maps[0]) if settings.output_maps else None,
                               ptr(maps[1]) if settings.output_maps else None, stream_handle(dev))
+            if want_grads and grads is None:
+                # set up after the raster launch (host time off the GPU's critical path); the
+                # fill itself starts after the binning, whose working set lives in L2
+                grads, grads_ready = _zeroed_grad_buffers(dev, n, sh, binned)
             st, K = binning_status(dev, n, cap, ntw, nth)
             if st == _lib.GSX_ERR_CAPACITY:
                 cap = int(K * 1.25) + 4096
@@ -320,6 +328,7 @@ class ViewPipeline:
             pr = None
             _bin_buffers(dev).release()
         st = dict(pr=pr, ids=ids, start=start, end=end, K=K, cap=cap, topleft=topleft, c2w_dev=c2w_dev,
+                  order=order if settings.bg is None and not settings.output_maps else None,
                   out=out, params=params, gcam=gcam, grad_flags=settings.grad_flags(), settings=settings,
                   counts=visible_counts)
         if settings.output_maps:
@@ -346,10 +355,14 @@ class ViewPipeline:
             g_alpha = torch.zeros((n,), dtype=torch.float32, device=dev)
             g_sh = torch.zeros_like(sh)
         with ev("raster_bwd"):
-            _lib.call("gsx_render_backward", ctypes.byref(state["params"]), n, state["cap"], ptr(pr.mean2d),
-                      ptr(pr.cov2d), ptr(sh), ptr(pr.alpha), ptr(state["start"]), ptr(state["end"]),
-                      ptr(state["ids"]), ptr(state["topleft"]), ptr(state["c2w_dev"]), ptr(state["out"]),
-                      ptr(grad_out), ptr(g_mean2d), ptr(g_cov2d), ptr(g_sh), ptr(g_alpha), stream_handle(dev))
+            common = (ctypes.byref(state["params"]), n, state["cap"], ptr(pr.mean2d), ptr(pr.cov2d), ptr(sh),
+                      ptr(pr.alpha), ptr(state["start"]), ptr(state["end"]), ptr(state["ids"]), ptr(state["topleft"]),
+                      ptr(state["c2w_dev"]), ptr(state["out"]), ptr(grad_out), ptr(g_mean2d), ptr(g_cov2d),
+                      ptr(g_sh), ptr(g_alpha))
+            if state.get("order") is not None:  # the forward's order (longest lists first)
+                _lib.call("gsx_render_backward_ordered", *common, ptr(state["order"]), stream_handle(dev))
+            else:
+                _lib.call("gsx_render_backward", *common, stream_handle(dev))
         g_mean = torch.empty_like(mean)
         g_q = torch.empty_like(qvec)
         g_ls = torch.empty_like(log_scale)
@@ -416,11 +429,12 @@ _copy_streams: dict = {}
 _fill_streams: dict = {}
 
 
-def _zeroed_grad_buffers(device, n: int, sh: torch.Tensor):
+def _zeroed_grad_buffers(device, n: int, sh: torch.Tensor, after: torch.cuda.Event):
     """The raster backward's accumulators (dL/dmean2d [n,2], dL/dcov2d [n,4],
     dL/dalpha [n], dL/dsh like sh), zero-filled on a side stream that starts
-    after the work already queued on the current stream; returns them and
-    the event the backward waits for."""
+    at `after` (an event of the current stream recorded before any kernel
+    that uses memory these fresh blocks may have held); returns them and the
+    event the backward waits for."""
     main = torch.cuda.current_stream(device)
     key = (device.type, device.index)
     if key not in _fill_streams:
@@ -430,7 +444,7 @@ def _zeroed_grad_buffers(device, n: int, sh: torch.Tensor):
             torch.empty((n, 4), dtype=torch.float32, device=device),
             torch.empty((n,), dtype=torch.float32, device=device),
             torch.empty(sh.shape, dtype=sh.dtype, device=device))
-    fs.wait_stream(main)  # the fresh blocks may still be read by queued work
+    fs.wait_event(after)
     done = torch.cuda.Event()
     with torch.cuda.stream(fs):
         for b in bufs:

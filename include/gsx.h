@@ -324,6 +324,25 @@ int gsx_render_forward_maps(const gsx_raster_params *params, int64_t n, int64_t 
                             float *out, const float *bg_rgb, const float *depth,
                             float *alpha_out, float *depth_out, void *stream);
 
+/*
+ * Scheduling order for the forward raster (no reference counterpart):
+ * tile_order i32[n_tiles] receives the tiles sorted by descending list length
+ * end - start, in log-spaced classes (8 per doubling; the order inside a
+ * class is unspecified).  Longest lists first shortens the tail of the grid.
+ */
+int gsx_tile_order(const int32_t *start, const int32_t *end, int32_t n_tiles, int32_t *tile_order,
+                   void *stream);
+
+/* gsx_render_forward with CTA b rendering tile tile_order[b]; tile_order must
+ * be a permutation of the n_tiles_w * n_tiles_h tiles (entries outside the
+ * grid render nothing).  The image does not depend on the order. */
+int gsx_render_forward_ordered(const gsx_raster_params *p, int64_t n, int64_t n_keys,
+                               const float *mean2d, const float *cov2d, const float *sh,
+                               const float *alpha, const int32_t *start, const int32_t *end,
+                               const int32_t *gaussian_ids, const float *topleft,
+                               const float *c2w, float *out, const int32_t *tile_order,
+                               void *stream);
+
 /* Backward raster; grad_* are added into (caller zeroes them). */
 int gsx_render_backward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
                         const float *mean2d, const float *cov2d, const float *sh,
@@ -342,6 +361,17 @@ int gsx_render_backward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
  * incomplete.  Synchronises `stream`; clear != 0 resets the bits.
  */
 int gsx_raster_status(uint32_t *flags, int32_t clear, void *stream);
+
+/* gsx_render_backward with CTA b working on tile tile_order[b] (the same
+ * contract as gsx_render_forward_ordered; the gradients do not depend on the
+ * order beyond the summation order of their float additions). */
+int gsx_render_backward_ordered(const gsx_raster_params *p, int64_t n, int64_t n_keys,
+                                const float *mean2d, const float *cov2d, const float *sh,
+                                const float *alpha, const int32_t *start, const int32_t *end,
+                                const int32_t *gaussian_ids, const float *topleft,
+                                const float *c2w, const float *out, const float *grad_out,
+                                float *grad_mean2d, float *grad_cov2d, float *grad_sh,
+                                float *grad_alpha, const int32_t *tile_order, void *stream);
 
 /*
  * Projection backward from the raster gradients grad_mean2d f32[n,2],

@@ -353,3 +353,4 @@ def test_17_bit_tile_ids_bitexact():
     np.testing.assert_array_equal(end.cpu().numpy(), ref["bins"]["end"])
     got = gpu_pipeline(wl, st, with_grad=False)
     assert_image_close(got["image"], ref["image"])
+
