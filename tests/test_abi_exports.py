@@ -70,3 +70,21 @@ def test_unaligned_binning_workspace_is_rejected_on_the_host():
     st = lib.gsx_bin_gaussians_async(n, fake, fake, fake, ntw, nth, cap, fake, fake, fake, fake + 16, need, None)
     assert st == _lib.GSX_ERR_INVALID_ARG
     assert b"256-byte aligned" in lib.gsx_last_error()
+
+
+def test_ordered_raster_entry_points_validate_on_the_host():
+    """The tile-order entry points refuse missing arguments before any CUDA
+    call (no GPU needed)."""
+    lib = _lib.load()
+    p = _lib.GsxRasterParams()
+    p.width, p.height, p.tile_w, p.tile_h, p.n_tiles_w, p.n_tiles_h = 16, 16, 16, 16, 1, 1
+    p.sh_order, p.sh_stride, p.pixel_size_x, p.pixel_size_y, p.T_thresh = 1, 1, 1.0, 1.0, 0.01
+    fake = 1 << 40
+    st = lib.gsx_render_forward_ordered(p, 1, 1, fake, fake, fake, fake, fake, fake, fake, fake, fake, fake,
+                                        None, None)
+    assert st == _lib.GSX_ERR_INVALID_ARG and b"tile_order" in lib.gsx_last_error()
+    st = lib.gsx_render_backward_ordered(p, 1, 1, *([fake] * 15), None, None)
+    assert st == _lib.GSX_ERR_INVALID_ARG and b"tile_order" in lib.gsx_last_error()
+    assert lib.gsx_tile_order(None, None, -1, None, None) == _lib.GSX_ERR_INVALID_ARG
+    assert lib.gsx_tile_order(None, None, 0, None, None) == _lib.GSX_OK
+    assert lib.gsx_tile_order(None, None, 4, None, None) == _lib.GSX_ERR_INVALID_ARG
