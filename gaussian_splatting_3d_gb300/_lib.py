@@ -133,6 +133,7 @@ SIGNATURES = {
         [POINTER(GsxRasterParams), c_int64, c_int64, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P],
     ),
     "gsx_raster_status": (c_int, [P, c_int32, P]),
+    "gsx_raster_wait_selftest": (c_int, [c_uint32, P, P]),
     "gsx_project_backward": (
         c_int,
         [c_int64, P, P, P, P, POINTER(GsxCamera), P, P, P, P, P, P, P, P, c_int32, P],

@@ -457,6 +457,13 @@ int gsx_render_backward_ordered(const gsx_raster_params *p, int64_t n, int64_t n
                          grad_alpha, tile_order, stream);
 }
 
+int gsx_raster_wait_selftest(uint32_t limit, uint32_t *polls_dev, void *stream) {
+  g_err[0] = 0;
+  GSX_REQUIRE(polls_dev, "null polls pointer");
+  GSX_REQUIRE(limit >= 1 && limit <= (1u << 20), "limit must be in [1, 2^20] (got %u)", limit);
+  return raster_wait_selftest(limit, polls_dev, as_stream(stream));
+}
+
 int gsx_raster_status(uint32_t *flags, int32_t clear, void *stream) {
   g_err[0] = 0;
   GSX_REQUIRE(flags, "null flags pointer");

@@ -157,6 +157,9 @@ int launch_raster_backward_batch(const RasterArgs &a, int C, int64_t total_tiles
 // Sticky error bits of the raster kernels (synchronises `s`); clear != 0
 // resets them.
 int raster_status(uint32_t *flags, int clear, cudaStream_t s);
+// One CTA waits on a barrier phase that cannot complete, for `limit` polls;
+// sets the raster timeout bit and writes the polls made to polls_dev[0].
+int raster_wait_selftest(uint32_t limit, uint32_t *polls_dev, cudaStream_t s);
 
 // Binning.  rect_tl/rect_br point at int32 pairs with `rect_stride` ints per
 // Gaussian (4 for packed [n,4] rects, 2 for separate [n,2] arrays).

@@ -404,6 +404,24 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32
       : "memory");
 }
 
+// Diagnostic of the bounded wait: one CTA polls a barrier phase that cannot
+// complete (two arrivals expected, one made, no copies), gives up after
+// `limit` polls and sets the same error bit as a raster whose bulk-copy wait
+// gave up.  out[0] = polls made by thread 0.
+__global__ void bounded_wait_selftest_kernel(uint32_t limit, uint32_t *out) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 2;" ::"r"(smem_u32(&bar)) : "memory");
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&bar)) : "memory");
+  }
+  __syncthreads();
+  uint32_t i = 0;
+  bool ok = false;
+  for (; i < limit && !ok; ++i) ok = mbar_try_wait(&bar, 0);
+  if (!ok) atomicOr(&g_raster_flags, kRasterErrTimeout);
+  if (threadIdx.x == 0) out[0] = i;
+}
+
 // The SH rows of this CTA's scene can be bulk-copied: every copy starts on a
 // 16-byte boundary and moves a multiple of 16 bytes (C*C and the row stride
 // multiples of 4 floats, base 16-byte aligned).
@@ -1211,6 +1229,12 @@ int launch_raster_forward_batch(const RasterArgs &a, int C, int64_t total_tiles,
 int launch_raster_backward_batch(const RasterArgs &a, int C, int64_t total_tiles, cudaStream_t s) {
   if (total_tiles == 0) return GSX_OK;
   return dispatch_bwd<true>(a, C, total_tiles, s);
+}
+
+int raster_wait_selftest(uint32_t limit, uint32_t *polls_dev, cudaStream_t s) {
+  count_launches(1);
+  bounded_wait_selftest_kernel<<<1, 32, 0, s>>>(limit, polls_dev);
+  return cuda_status(cudaGetLastError(), "bounded_wait_selftest_kernel launch");
 }
 
 int raster_status(uint32_t *flags, int clear, cudaStream_t s) {

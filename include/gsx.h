@@ -362,6 +362,15 @@ int gsx_render_backward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
  */
 int gsx_raster_status(uint32_t *flags, int32_t clear, void *stream);
 
+/*
+ * Diagnostic of the failure path above (no reference counterpart): one CTA
+ * polls a barrier phase that cannot complete, gives up after `limit` polls
+ * (1 <= limit <= 2^20), sets bit 0 of the raster status and writes the polls
+ * made to polls_dev[0] (device memory).  Nothing faults or hangs; the context
+ * stays usable.
+ */
+int gsx_raster_wait_selftest(uint32_t limit, uint32_t *polls_dev, void *stream);
+
 /* gsx_render_backward with CTA b working on tile tile_order[b] (the same
  * contract as gsx_render_forward_ordered; the gradients do not depend on the
  * order beyond the summation order of their float additions). */
