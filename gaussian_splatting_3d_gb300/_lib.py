@@ -134,6 +134,8 @@ SIGNATURES = {
     ),
     "gsx_raster_status": (c_int, [P, c_int32, P]),
     "gsx_raster_wait_selftest": (c_int, [c_uint32, P, P]),
+    "gsx_look_back_selftest_bytes": (c_size_t, []),
+    "gsx_look_back_selftest": (c_int, [P, c_size_t, P, P]),
     "gsx_project_backward": (
         c_int,
         [c_int64, P, P, P, P, POINTER(GsxCamera), P, P, P, P, P, P, P, P, c_int32, P],

@@ -151,6 +151,14 @@ int gsx_bin_gaussians_async(int64_t n, const int32_t *rect, const int32_t *count
                            as_stream(stream));
 }
 
+size_t gsx_look_back_selftest_bytes(void) { return look_back_selftest_bytes(); }
+
+int gsx_look_back_selftest(void *scratch, size_t scratch_bytes, uint32_t *error_bits, void *stream) {
+  g_err[0] = 0;
+  GSX_REQUIRE(scratch, "null scratch");
+  return look_back_selftest(scratch, scratch_bytes, error_bits, as_stream(stream));
+}
+
 int gsx_binning_status(const void *workspace, int64_t n_gaussians, int64_t key_capacity,
                        int32_t n_tiles_w, int32_t n_tiles_h, int64_t *n_keys_out,
                        void *stream) {

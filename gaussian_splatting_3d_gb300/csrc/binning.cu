@@ -620,6 +620,50 @@ size_t binning_workspace_bytes(int64_t n, int64_t cap, int64_t n_tiles) {
   return carve_ws(nullptr, n, cap).bytes;
 }
 
+// Diagnostic of the look-back's bounded wait: one onesweep pass of 2 chunks
+// launched as a single CTA whose ticket is preset to 1, so it claims chunk 1
+// and waits for chunk 0, which no CTA ever publishes.  The wait gives up after
+// its poll limit, sets the timeout bit and the CTA finishes its pass.
+// `scratch` (>= look_back_selftest_bytes()) is caller device memory; returns
+// the binning status the timeout maps to (GSX_ERR_TIMEOUT when it works).
+size_t look_back_selftest_bytes() { return align256(4 * (size_t)kTile * 2 * 4) + 4 * 256 * 2 * 2 + 64; }
+
+int look_back_selftest(void *scratch, size_t bytes, uint32_t *error_host, cudaStream_t s) {
+  if (bytes < look_back_selftest_bytes()) {
+    set_error("self-test scratch too small: %zu < %zu bytes", bytes, look_back_selftest_bytes());
+    return GSX_ERR_CAPACITY;
+  }
+  if ((reinterpret_cast<uintptr_t>(scratch) & 255) != 0) {
+    set_error("self-test scratch must be 256-byte aligned");
+    return GSX_ERR_INVALID_ARG;
+  }
+  const uint32_t n = 2 * kTile;
+  char *p = static_cast<char *>(scratch);
+  uint32_t *keys_in = reinterpret_cast<uint32_t *>(p);
+  uint32_t *keys_out = keys_in + n, *vals_in = keys_in + 2 * n, *vals_out = keys_in + 3 * n;
+  char *state = p + align256(4 * (size_t)n * 4);
+  uint32_t *hist = reinterpret_cast<uint32_t *>(state);          // [256]
+  uint32_t *status = hist + 256;                                 // [2 chunks][256]
+  uint32_t *ticket = status + 2 * 256, *error = ticket + 1;
+  cudaError_t e = cudaMemsetAsync(p, 0, look_back_selftest_bytes(), s);
+  const uint32_t one = 1;
+  // the histogram of 2*kTile zero keys: all in digit 0
+  const uint32_t h0 = n;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(ticket, &one, 4, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hist, &h0, 4, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_status(e, "look-back self-test set-up");
+  count_launches(1);
+  onesweep_kernel<8, kItems><<<1, kThreads, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n, nullptr, 0, hist,
+                                         status, ticket, error);
+  e = cudaGetLastError();
+  uint32_t err = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&err, error, 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_status(e, "look-back self-test");
+  if (error_host) *error_host = err;
+  return decode_binning_status(0, err, 0, 1, 1);
+}
+
 // Enqueue the whole binning on `s` without synchronising.  Keys beyond
 // `capacity` are not written; the key total and the error bits stay in the
 // workspace for binning_status.

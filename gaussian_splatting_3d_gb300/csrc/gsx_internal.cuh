@@ -176,6 +176,8 @@ int copy_binning_status_async(const void *ws, int64_t n, int64_t capacity, void 
                               cudaStream_t s);
 int decode_binning_status(unsigned long long total, uint32_t error_bits, int64_t capacity,
                           int32_t n_tiles_w, int32_t n_tiles_h);
+size_t look_back_selftest_bytes();
+int look_back_selftest(void *scratch, size_t bytes, uint32_t *error_host, cudaStream_t s);
 int run_binning(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
                 int32_t rect_stride, const int32_t *counts, const float *depth,
                 int32_t n_tiles_w, int32_t n_tiles_h, int64_t capacity,

@@ -268,6 +268,17 @@ int gsx_bin_gaussians_async(int64_t n, const int32_t *rect, const int32_t *count
                             int64_t key_capacity, int32_t *gaussian_ids, int32_t *start,
                             int32_t *end, void *workspace, size_t workspace_bytes,
                             void *stream);
+/*
+ * Diagnostic of the sort's bounded look-back wait (no reference counterpart):
+ * a single CTA claims chunk 1 of a two-chunk pass and waits for chunk 0,
+ * which never publishes; the wait gives up after its poll limit and sets the
+ * timeout bit.  Returns GSX_ERR_TIMEOUT when the path works (error_bits, if
+ * not NULL, receives the raw bits).  Synchronises `stream`; scratch is
+ * caller device memory of gsx_look_back_selftest_bytes(), 256-byte aligned.
+ */
+size_t gsx_look_back_selftest_bytes(void);
+int gsx_look_back_selftest(void *scratch, size_t scratch_bytes, uint32_t *error_bits, void *stream);
+
 int gsx_binning_status(const void *workspace, int64_t n_gaussians, int64_t key_capacity,
                        int32_t n_tiles_w, int32_t n_tiles_h, int64_t *n_keys_out,
                        void *stream);

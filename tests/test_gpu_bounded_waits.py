@@ -45,3 +45,25 @@ def test_selftest_limit_is_validated_on_the_host():
     lib = _lib.load()
     assert lib.gsx_raster_wait_selftest(0, ctypes.c_void_p(1 << 40), None) == _lib.GSX_ERR_INVALID_ARG
     assert lib.gsx_raster_wait_selftest((1 << 20) + 1, ctypes.c_void_p(1 << 40), None) == _lib.GSX_ERR_INVALID_ARG
+
+
+def test_sort_look_back_wait_gives_up_and_reports():
+    """A onesweep chunk whose predecessor never publishes stops waiting after
+    its poll limit: the pass reports GSX_ERR_TIMEOUT and the device stays
+    usable (a binning afterwards is exact)."""
+    dev = torch.device("cuda:0")
+    lib = _lib.load()
+    scratch = torch.empty(lib.gsx_look_back_selftest_bytes(), dtype=torch.uint8, device=dev)
+    bits = ctypes.c_uint32(0)
+    st = lib.gsx_look_back_selftest(ptr(scratch), scratch.numel(), ctypes.byref(bits), stream_handle(dev))
+    assert st == _lib.GSX_ERR_TIMEOUT, lib.gsx_last_error()
+    assert bits.value & 1
+    wl = S.custom_workload(2000, 96, 64, 1, seed=53)
+    ref = O.render_view(wl.scene, wl.views[0])
+    pr = ref["proj"]
+    t = lambda a, dt=torch.float32: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dt)  # noqa: E731
+    proj = renderer.Projected(t(pr["mean2d"]), t(pr["cov2d"]), t(pr["depth"]), t(pr["alpha"]),
+                              t(pr["rect"], torch.int32), t(pr["counts"], torch.int32))
+    ids, start, end, K = renderer.bin_gaussians(proj, 6, 4)
+    assert K == ref["bins"]["K"]
+    np.testing.assert_array_equal(ids.cpu().numpy(), ref["bins"]["ids"])
