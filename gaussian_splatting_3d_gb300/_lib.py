@@ -116,6 +116,10 @@ SIGNATURES = {
         [POINTER(GsxRasterParams), c_int64, c_int64, P, P, P, P, P, P, P, P, P, P, P],
     ),
     "gsx_tile_order": (c_int, [P, P, c_int32, P, P]),
+    "gsx_project_colors": (c_int, [c_int64, P, P, c_int32, c_int32, P, P, P, P]),
+    "gsx_project_colors_backward": (c_int, [c_int64, P, P, c_int32, c_int32, P, P, P, P, P, P, P]),
+    "gsx_render_forward_rgb": (c_int, [POINTER(GsxRasterParams), c_int64, c_int64] + [P] * 12),
+    "gsx_render_backward_rgb": (c_int, [POINTER(GsxRasterParams), c_int64, c_int64] + [P] * 17),
     "gsx_render_forward_ordered": (
         c_int,
         [POINTER(GsxRasterParams), c_int64, c_int64, P, P, P, P, P, P, P, P, P, P, P, P],

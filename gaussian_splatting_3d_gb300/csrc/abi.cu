@@ -378,6 +378,105 @@ int gsx_render_forward_ordered(const gsx_raster_params *p, int64_t n, int64_t n_
                         c2w, out, nullptr, nullptr, nullptr, nullptr, tile_order, stream);
 }
 
+int gsx_render_forward_rgb(const gsx_raster_params *p, int64_t n, int64_t n_keys,
+                           const float *mean2d, const float *cov2d, const float *rgb,
+                           const float *alpha, const int32_t *start, const int32_t *end,
+                           const int32_t *gaussian_ids, const float *topleft, const float *c2w,
+                           float *out, const int32_t *tile_order, void *stream) {
+  g_err[0] = 0;
+  GSX_REQUIRE(p, "null params");
+  RasterArgs a = make_args(p->tile_w, p->tile_h, (uint32_t)p->n_tiles_w,
+                           (uint32_t)p->n_tiles_h, p->pixel_size_x, p->pixel_size_y,
+                           (uint32_t)p->height, (uint32_t)p->width, p->T_thresh);
+  a.sh_stride = 1;  // rgb [n,3] as one coefficient per channel
+  a.mean2d = mean2d;
+  a.cov2d = cov2d;
+  a.sh = rgb;
+  a.alpha = alpha;
+  a.start = start;
+  a.end = end;
+  a.ids = gaussian_ids;
+  a.topleft = topleft;
+  a.c2w = c2w;
+  a.out = out;
+  a.write_empty = p->write_empty_tiles;
+  a.n = n;
+  a.n_keys = n_keys;
+  a.tile_order = tile_order;
+  int st = check_raster(a, 1, n, n_keys);
+  if (st != GSX_OK) return st;
+  return launch_raster_forward_rgb(a, as_stream(stream));
+}
+
+int gsx_render_backward_rgb(const gsx_raster_params *p, int64_t n, int64_t n_keys,
+                            const float *mean2d, const float *cov2d, const float *rgb,
+                            const float *alpha, const int32_t *start, const int32_t *end,
+                            const int32_t *gaussian_ids, const float *topleft, const float *c2w,
+                            const float *out, const float *grad_out, float *grad_mean2d,
+                            float *grad_cov2d, float *grad_rgb, float *grad_alpha,
+                            const int32_t *tile_order, void *stream) {
+  g_err[0] = 0;
+  GSX_REQUIRE(p, "null params");
+  RasterArgs a = make_args(p->tile_w, p->tile_h, (uint32_t)p->n_tiles_w,
+                           (uint32_t)p->n_tiles_h, p->pixel_size_x, p->pixel_size_y,
+                           (uint32_t)p->height, (uint32_t)p->width, p->T_thresh);
+  a.sh_stride = 1;
+  a.mean2d = mean2d;
+  a.cov2d = cov2d;
+  a.sh = rgb;
+  a.alpha = alpha;
+  a.start = start;
+  a.end = end;
+  a.ids = gaussian_ids;
+  a.topleft = topleft;
+  a.c2w = c2w;
+  a.out = const_cast<float *>(out);
+  a.final_img = out;
+  a.grad_out = grad_out;
+  a.g_mean2d = grad_mean2d;
+  a.g_cov2d = grad_cov2d;
+  a.g_sh = grad_rgb;
+  a.g_alpha = grad_alpha;
+  a.n = n;
+  a.n_keys = n_keys;
+  a.tile_order = tile_order;
+  int st = check_raster(a, 1, n, n_keys);
+  if (st != GSX_OK) return st;
+  GSX_REQUIRE(grad_out && (n == 0 || (grad_mean2d && grad_cov2d && grad_rgb && grad_alpha)),
+              "null gradient pointer");
+  return launch_raster_backward_rgb(a, as_stream(stream));
+}
+
+int gsx_project_colors(int64_t n, const float *mean, const float *sh, int32_t sh_stride,
+                       int32_t sh_order, const float *cam_pos, const int32_t *counts, float *rgb,
+                       void *stream) {
+  g_err[0] = 0;
+  GSX_REQUIRE(n >= 0, "n must be >= 0 (got %lld)", (long long)n);
+  if (n == 0) return GSX_OK;
+  GSX_REQUIRE(mean && sh && cam_pos && rgb, "null pointer argument");
+  GSX_REQUIRE(sh_order >= 1 && sh_order <= 4, "SH order C must be 1..4 (got %d)", sh_order);
+  GSX_REQUIRE(sh_stride >= sh_order * sh_order, "sh_stride %d < C*C = %d", sh_stride,
+              sh_order * sh_order);
+  return launch_colors_forward(n, mean, sh, sh_stride, sh_order, cam_pos, counts, rgb,
+                               as_stream(stream));
+}
+
+int gsx_project_colors_backward(int64_t n, const float *mean, const float *sh, int32_t sh_stride,
+                                int32_t sh_order, const float *cam_pos, const int32_t *counts,
+                                const float *rgb, const float *grad_rgb, float *grad_sh,
+                                float *grad_mean, void *stream) {
+  g_err[0] = 0;
+  GSX_REQUIRE(n >= 0, "n must be >= 0 (got %lld)", (long long)n);
+  if (n == 0) return GSX_OK;
+  GSX_REQUIRE(mean && sh && cam_pos && rgb && grad_rgb && grad_sh && grad_mean,
+              "null pointer argument");
+  GSX_REQUIRE(sh_order >= 1 && sh_order <= 4, "SH order C must be 1..4 (got %d)", sh_order);
+  GSX_REQUIRE(sh_stride >= sh_order * sh_order, "sh_stride %d < C*C = %d", sh_stride,
+              sh_order * sh_order);
+  return launch_colors_backward(n, mean, sh, sh_stride, sh_order, cam_pos, counts, rgb, grad_rgb,
+                                grad_sh, grad_mean, as_stream(stream));
+}
+
 int gsx_tile_order(const int32_t *start, const int32_t *end, int32_t n_tiles, int32_t *tile_order,
                    void *stream) {
   g_err[0] = 0;

@@ -95,6 +95,16 @@ int launch_project_backward_batch(const gsx_batch_view *views, int32_t n_views, 
                                   const float *g_cov2d, const float *g_alpha, int32_t flags,
                                   cudaStream_t s);
 
+// Opt-in per-Gaussian colours (colors.cu): rgb [n,3] from the direction
+// camera centre -> mean; the backward overwrites g_sh [n,3,sh_stride] and adds
+// the direction's share of the gradient into g_mean [n,3].
+int launch_colors_forward(int64_t n, const float *mean, const float *sh, int sh_stride, int C,
+                          const float *cam_pos_host, const int32_t *counts, float *rgb,
+                          cudaStream_t s);
+int launch_colors_backward(int64_t n, const float *mean, const float *sh, int sh_stride, int C,
+                           const float *cam_pos_host, const int32_t *counts, const float *rgb,
+                           const float *g_rgb, float *g_sh, float *g_mean, cudaStream_t s);
+
 // Adaptive density control (densify.cu).
 int launch_count_visible(int64_t n, const int32_t *counts, int32_t *cnt, cudaStream_t s);
 int launch_accumulate_norm(int64_t n, const float *grad, int dim, const int32_t *counts,
@@ -150,6 +160,10 @@ int launch_raster_forward(const RasterArgs &a, int C, cudaStream_t s);
 int launch_tile_order(const int32_t *start, const int32_t *end, int32_t n_tiles, int32_t *order,
                       cudaStream_t s);
 int launch_raster_backward(const RasterArgs &a, int C, cudaStream_t s);
+// Per-Gaussian colours: a.sh = rgb [n,3] (a.sh_stride = 1); the backward adds
+// dL/drgb into a.g_sh.
+int launch_raster_forward_rgb(const RasterArgs &a, cudaStream_t s);
+int launch_raster_backward_rgb(const RasterArgs &a, cudaStream_t s);
 // Batched: a.views/a.n_views set, grid = total tiles (all views share the tile
 // shape and SH order; the per-view fields of `a` are ignored).
 int launch_raster_forward_batch(const RasterArgs &a, int C, int64_t total_tiles, cudaStream_t s);

@@ -577,7 +577,10 @@ __device__ __forceinline__ void pack_basis(const float *Y, float2 *Y2) {
 }
 
 // EXTRAS: background colour and alpha / depth maps (single view only).
-template <int C, int MAXT, bool BATCHED, bool EXTRAS>
+// RGB: per-Gaussian colours (an opt-in mode; the reference evaluates SH per
+// pixel): `sh` holds rgb [n,3] as C = 1 rows, the basis is the constant 1
+// and the colour is the stored value itself.
+template <int C, int MAXT, bool BATCHED, bool EXTRAS, bool RGB = false>
 __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a) {
   constexpr int GSH = Sh<C>::GSH, CCP = Sh<C>::CCP;
   extern __shared__ float4 smem4[];
@@ -616,7 +619,8 @@ __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a
   float2 Y2[Sh<C>::NY2];
   {
     float Y[Sh<C>::CC];
-    sh_basis<C>(ctx.c2w, px, py, Y);
+    if constexpr (RGB) Y[0] = 1.0f;
+    else sh_basis<C>(ctx.c2w, px, py, Y);
     pack_basis<C>(Y, Y2);
   }
   float o0 = 0.0f, o1 = 0.0f, o2 = 0.0f, T = 1.0f, dsum = 0.0f;
@@ -656,9 +660,16 @@ __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a
         if (al * G < kMinRenderAlpha) continue;
         if (isnan(coeff)) coeff = 0.0f;
         const float *s = L.sh + i * GSH;
-        float y0 = fast_sigmoid(sh_logit<C>(s, Y2));
-        float y1 = fast_sigmoid(sh_logit<C>(s + CCP, Y2));
-        float y2 = fast_sigmoid(sh_logit<C>(s + 2 * CCP, Y2));
+        float y0, y1, y2;
+        if constexpr (RGB) {
+          y0 = s[0];
+          y1 = s[CCP];
+          y2 = s[2 * CCP];
+        } else {
+          y0 = fast_sigmoid(sh_logit<C>(s, Y2));
+          y1 = fast_sigmoid(sh_logit<C>(s + CCP, Y2));
+          y2 = fast_sigmoid(sh_logit<C>(s + 2 * CCP, Y2));
+        }
         // coeff is finite here, so y * coeff is NaN exactly when y is; fmaxf
         // returns its non-NaN operand and y >= 0, so this is the reference's
         // `if isnan(y * coeff) y = 0`
@@ -806,7 +817,9 @@ __device__ __forceinline__ void flush_sh_group(const float *Ws, const float *Ys,
     }
 }
 
-template <int C, int MAXT, bool BATCHED>
+// RGB: as in the forward; the gradient staged for the C = 1 reduction is
+// then dL/drgb itself (the constant basis makes the product a plain sum).
+template <int C, int MAXT, bool BATCHED, bool RGB = false>
 __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1)
     raster_backward_kernel(const RasterArgs a) {
   constexpr int CC = Sh<C>::CC, CCP = Sh<C>::CCP, GSH = Sh<C>::GSH;
@@ -842,7 +855,8 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
   int *slots = s_slots + warp * 8;
   {
     float Y[CC];
-    sh_basis<C>(ctx.c2w, px, py, Y);
+    if constexpr (RGB) Y[0] = 1.0f;
+    else sh_basis<C>(ctx.c2w, px, py, Y);
     pack_basis<C>(Y, Y2);
 #pragma unroll
     for (int k = 0; k < 16; ++k) Ys[k * kYStride + lane] = k < CC ? Y[k < CC ? k : 0] : 0.0f;
@@ -904,11 +918,13 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
               float y[3];
 #pragma unroll
               for (int ch = 0; ch < 3; ++ch) {
-                y[ch] = fmaxf(fast_sigmoid(sh_logit<C>(s + ch * CCP, Y2)), 0.0f);  // NaN -> 0
+                y[ch] = RGB ? fmaxf(s[ch * CCP], 0.0f)
+                            : fmaxf(fast_sigmoid(sh_logit<C>(s + ch * CCP, Y2)), 0.0f);  // NaN -> 0
                 o[ch] = fmaf(coeff, y[ch], o[ch]);
               }
 #pragma unroll
-              for (int ch = 0; ch < 3; ++ch) w[ch] = coeff * (y[ch] * (1.0f - y[ch])) * go[ch];
+              for (int ch = 0; ch < 3; ++ch)
+                w[ch] = RGB ? coeff * go[ch] : coeff * (y[ch] * (1.0f - y[ch])) * go[ch];
               const float one_m = fmaf(-al, G, 1.0f);
               float inv_one_m;  // gradient path only: the hardware reciprocal (1 ulp)
               asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv_one_m) : "f"(one_m));
@@ -1038,16 +1054,16 @@ cudaError_t ensure_smem(K kernel, size_t smem, size_t &done) {
   return e;
 }
 
-template <int C, int MAXT, bool BATCHED, bool EXTRAS>
+template <int C, int MAXT, bool BATCHED, bool EXTRAS, bool RGB = false>
 int launch_fwd_tt(RasterArgs a, int64_t grid, cudaStream_t s) {
   const int nthr = block_threads(a);
   a.batch = nthr < 128 ? nthr : 128;
   const size_t smem = fwd_smem<C>(a.batch, nthr);
   static size_t attr_done = 0;
-  cudaError_t e = ensure_smem(raster_forward_kernel<C, MAXT, BATCHED, EXTRAS>, smem, attr_done);
+  cudaError_t e = ensure_smem(raster_forward_kernel<C, MAXT, BATCHED, EXTRAS, RGB>, smem, attr_done);
   if (e != cudaSuccess) return cuda_status(e, "raster_forward smem attribute");
   count_launches(1);
-  raster_forward_kernel<C, MAXT, BATCHED, EXTRAS><<<(unsigned)grid, nthr, smem, s>>>(a);
+  raster_forward_kernel<C, MAXT, BATCHED, EXTRAS, RGB><<<(unsigned)grid, nthr, smem, s>>>(a);
   return cuda_status(cudaGetLastError(), "raster_forward_kernel launch");
 }
 
@@ -1062,7 +1078,7 @@ int launch_fwd_t(const RasterArgs &a, int64_t grid, cudaStream_t s) {
                                  : launch_fwd_tt<C, 1024, BATCHED, false>(a, grid, s);
 }
 
-template <int C, int MAXT, bool BATCHED>
+template <int C, int MAXT, bool BATCHED, bool RGB = false>
 int launch_bwd_tt(RasterArgs a, int64_t grid, cudaStream_t s) {
   const int nthr = block_threads(a);
   a.vec_grads = ((reinterpret_cast<uintptr_t>(a.g_mean2d) & 7) == 0 &&
@@ -1072,10 +1088,10 @@ int launch_bwd_tt(RasterArgs a, int64_t grid, cudaStream_t s) {
   a.batch = nthr < 64 ? nthr : 64;
   const size_t smem = bwd_smem<C>(a.batch, nthr);
   static size_t attr_done = 0;
-  cudaError_t e = ensure_smem(raster_backward_kernel<C, MAXT, BATCHED>, smem, attr_done);
+  cudaError_t e = ensure_smem(raster_backward_kernel<C, MAXT, BATCHED, RGB>, smem, attr_done);
   if (e != cudaSuccess) return cuda_status(e, "raster_backward smem attribute");
   count_launches(1);
-  raster_backward_kernel<C, MAXT, BATCHED><<<(unsigned)grid, nthr, smem, s>>>(a);
+  raster_backward_kernel<C, MAXT, BATCHED, RGB><<<(unsigned)grid, nthr, smem, s>>>(a);
   return cuda_status(cudaGetLastError(), "raster_backward_kernel launch");
 }
 
@@ -1213,6 +1229,20 @@ int launch_raster_forward(const RasterArgs &a, int C, cudaStream_t s) {
   const int64_t grid = (int64_t)a.n_tiles_w * a.n_tiles_h;
   if (grid == 0) return GSX_OK;
   return dispatch_fwd<false>(a, C, grid, s);
+}
+
+int launch_raster_forward_rgb(const RasterArgs &a, cudaStream_t s) {
+  const int64_t grid = (int64_t)a.n_tiles_w * a.n_tiles_h;
+  if (grid == 0) return GSX_OK;
+  return block_threads(a) <= 256 ? launch_fwd_tt<1, 256, false, false, true>(a, grid, s)
+                                 : launch_fwd_tt<1, 1024, false, false, true>(a, grid, s);
+}
+
+int launch_raster_backward_rgb(const RasterArgs &a, cudaStream_t s) {
+  const int64_t grid = (int64_t)a.n_tiles_w * a.n_tiles_h;
+  if (grid == 0) return GSX_OK;
+  return block_threads(a) <= 256 ? launch_bwd_tt<1, 256, false, true>(a, grid, s)
+                                 : launch_bwd_tt<1, 1024, false, true>(a, grid, s);
 }
 
 int launch_raster_backward(const RasterArgs &a, int C, cudaStream_t s) {

@@ -82,6 +82,11 @@ class RasterSettings:
     # reference's default bg=False) and per-pixel alpha / depth maps
     bg: tuple | None = None
     output_maps: bool = False
+    # "pixel": SH evaluated per pixel from the pixel's ray (the reference);
+    # "gaussian": one colour per Gaussian per view from the direction camera
+    # centre -> mean, computed once in the projection (opt-in, not the
+    # reference's images)
+    sh_mode: str = "pixel"
 
     def grad_flags(self) -> int:
         if self.exact_grad:
@@ -267,6 +272,11 @@ class ViewPipeline:
         n = mean.shape[0]
         sh_stride = sh.shape[-1]
         C = settings.sh_order or int(round(sh_stride ** 0.5))
+        rgb_mode = settings.sh_mode == "gaussian"
+        if settings.sh_mode not in ("pixel", "gaussian"):
+            raise ValueError(f"sh_mode must be 'pixel' or 'gaussian' (got {settings.sh_mode!r})")
+        if rgb_mode and (settings.bg is not None or settings.output_maps):
+            raise NotImplementedError("per-Gaussian colours composite no background and write no maps")
         gcam = make_gsx_camera(c2w_np, cam)
         ev = timer.stage if timer is not None else (lambda name: _null_ctx())
         with ev("project"):
@@ -279,6 +289,8 @@ class ViewPipeline:
         order = torch.empty((ntw * nth,), dtype=torch.int32, device=dev)
         params = _raster_params(cam, settings, C, sh_stride)
         grads = grads_ready = None
+        rgb = None
+        cam_pos = (ctypes.c_float * 3)(*[float(v) for v in np.asarray(c2w_np, np.float32).reshape(3, 4)[:, 3]])
         cap = max(self.key_capacity, 1 << 16)
         want_grads = prepare_grads and not settings.recompute_projection
         for _ in range(3):
@@ -289,8 +301,18 @@ class ViewPipeline:
                 binned.record(torch.cuda.current_stream(dev))
             if sh_ready is not None:  # only the raster reads the SH coefficients
                 torch.cuda.current_stream(dev).wait_event(sh_ready)
+            if rgb_mode and rgb is None:
+                with ev("colors"):
+                    rgb = torch.empty((n, 3), dtype=torch.float32, device=dev)
+                    _lib.call("gsx_project_colors", n, ptr(mean), ptr(sh), sh_stride, C, ctypes.addressof(cam_pos),
+                              ptr(pr.counts), ptr(rgb), stream_handle(dev))
             with ev("raster_fwd"):
-                if settings.bg is None and not settings.output_maps:
+                if rgb_mode:
+                    _lib.call("gsx_tile_order", ptr(start), ptr(end), ntw * nth, ptr(order), stream_handle(dev))
+                    _lib.call("gsx_render_forward_rgb", ctypes.byref(params), n, cap, ptr(pr.mean2d), ptr(pr.cov2d),
+                              ptr(rgb), ptr(pr.alpha), ptr(start), ptr(end), ptr(ids), ptr(topleft), ptr(c2w_dev),
+                              ptr(out), ptr(order), stream_handle(dev))
+                elif settings.bg is None and not settings.output_maps:
                     # longest tile lists first: the order changes the schedule, not the image
                     _lib.call("gsx_tile_order", ptr(start), ptr(end), ntw * nth, ptr(order), stream_handle(dev))
                     _lib.call("gsx_render_forward_ordered", ctypes.byref(params), n, cap, ptr(pr.mean2d),
@@ -309,7 +331,7 @@ class ViewPipeline:
             if want_grads and grads is None:
                 # set up after the raster launch (host time off the GPU's critical path); the
                 # fill itself starts after the binning, whose working set lives in L2
-                grads, grads_ready = _zeroed_grad_buffers(dev, n, sh, binned)
+                grads, grads_ready = _zeroed_grad_buffers(dev, n, (n, 3) if rgb_mode else tuple(sh.shape), binned)
             st, K = binning_status(dev, n, cap, ntw, nth)
             if st == _lib.GSX_ERR_CAPACITY:
                 cap = int(K * 1.25) + 4096
@@ -329,6 +351,7 @@ class ViewPipeline:
             _bin_buffers(dev).release()
         st = dict(pr=pr, ids=ids, start=start, end=end, K=K, cap=cap, topleft=topleft, c2w_dev=c2w_dev,
                   order=order if settings.bg is None and not settings.output_maps else None,
+                  rgb=rgb, cam_pos=cam_pos, C=C,
                   out=out, params=params, gcam=gcam, grad_flags=settings.grad_flags(), settings=settings,
                   counts=visible_counts)
         if settings.output_maps:
@@ -346,20 +369,24 @@ class ViewPipeline:
             with ev("project_recompute"):
                 pr = project(mean, qvec, log_scale, alpha_logit, state["gcam"], state["settings"])
         grad_out = grad_out.contiguous()
-        if state.get("grads") is not None and state["grads"][3].shape == sh.shape:
+        rgb = state.get("rgb")
+        acc_shape = (n, 3) if rgb is not None else tuple(sh.shape)  # dL/drgb or dL/dsh accumulator
+        if state.get("grads") is not None and tuple(state["grads"][3].shape) == acc_shape:
             torch.cuda.current_stream(dev).wait_event(state["grads_ready"])
-            g_mean2d, g_cov2d, g_alpha, g_sh = state.pop("grads")
+            g_mean2d, g_cov2d, g_alpha, g_acc = state.pop("grads")
         else:
             g_mean2d = torch.zeros((n, 2), dtype=torch.float32, device=dev)
             g_cov2d = torch.zeros((n, 4), dtype=torch.float32, device=dev)
             g_alpha = torch.zeros((n,), dtype=torch.float32, device=dev)
-            g_sh = torch.zeros_like(sh)
+            g_acc = torch.zeros(acc_shape, dtype=torch.float32, device=dev)
         with ev("raster_bwd"):
-            common = (ctypes.byref(state["params"]), n, state["cap"], ptr(pr.mean2d), ptr(pr.cov2d), ptr(sh),
-                      ptr(pr.alpha), ptr(state["start"]), ptr(state["end"]), ptr(state["ids"]), ptr(state["topleft"]),
-                      ptr(state["c2w_dev"]), ptr(state["out"]), ptr(grad_out), ptr(g_mean2d), ptr(g_cov2d),
-                      ptr(g_sh), ptr(g_alpha))
-            if state.get("order") is not None:  # the forward's order (longest lists first)
+            common = (ctypes.byref(state["params"]), n, state["cap"], ptr(pr.mean2d), ptr(pr.cov2d),
+                      ptr(rgb if rgb is not None else sh), ptr(pr.alpha), ptr(state["start"]), ptr(state["end"]),
+                      ptr(state["ids"]), ptr(state["topleft"]), ptr(state["c2w_dev"]), ptr(state["out"]),
+                      ptr(grad_out), ptr(g_mean2d), ptr(g_cov2d), ptr(g_acc), ptr(g_alpha))
+            if rgb is not None:
+                _lib.call("gsx_render_backward_rgb", *common, ptr(state["order"]), stream_handle(dev))
+            elif state.get("order") is not None:  # the forward's order (longest lists first)
                 _lib.call("gsx_render_backward_ordered", *common, ptr(state["order"]), stream_handle(dev))
             else:
                 _lib.call("gsx_render_backward", *common, stream_handle(dev))
@@ -371,6 +398,14 @@ class ViewPipeline:
             _lib.call("gsx_project_backward", n, ptr(mean), ptr(qvec), ptr(log_scale), ptr(alpha_logit),
                       ctypes.byref(state["gcam"]), ptr(pr.counts), ptr(g_mean2d), ptr(g_cov2d), ptr(g_alpha),
                       ptr(g_mean), ptr(g_q), ptr(g_ls), ptr(g_al), state["grad_flags"], stream_handle(dev))
+        if rgb is not None:  # dL/drgb -> dL/dsh, and the view direction's share of dL/dmean
+            g_sh = torch.empty_like(sh)
+            with ev("colors_bwd"):
+                _lib.call("gsx_project_colors_backward", n, ptr(mean), ptr(sh), sh.shape[-1], state["C"],
+                          ctypes.addressof(state["cam_pos"]), ptr(pr.counts), ptr(rgb), ptr(g_acc), ptr(g_sh),
+                          ptr(g_mean), stream_handle(dev))
+        else:
+            g_sh = g_acc
         state["g_mean2d"] = g_mean2d  # dL/dmean2d (normalised image coordinates), for densification
         return g_mean, g_q, g_ls, g_sh, g_al
 
@@ -429,12 +464,12 @@ _copy_streams: dict = {}
 _fill_streams: dict = {}
 
 
-def _zeroed_grad_buffers(device, n: int, sh: torch.Tensor, after: torch.cuda.Event):
+def _zeroed_grad_buffers(device, n: int, acc_shape: tuple, after: torch.cuda.Event):
     """The raster backward's accumulators (dL/dmean2d [n,2], dL/dcov2d [n,4],
-    dL/dalpha [n], dL/dsh like sh), zero-filled on a side stream that starts
-    at `after` (an event of the current stream recorded before any kernel
-    that uses memory these fresh blocks may have held); returns them and the
-    event the backward waits for."""
+    dL/dalpha [n], and dL/dsh or dL/drgb of shape acc_shape), zero-filled on a
+    side stream that starts at `after` (an event of the current stream
+    recorded before any kernel that uses memory these fresh blocks may have
+    held); returns them and the event the backward waits for."""
     main = torch.cuda.current_stream(device)
     key = (device.type, device.index)
     if key not in _fill_streams:
@@ -443,7 +478,7 @@ def _zeroed_grad_buffers(device, n: int, sh: torch.Tensor, after: torch.cuda.Eve
     bufs = (torch.empty((n, 2), dtype=torch.float32, device=device),
             torch.empty((n, 4), dtype=torch.float32, device=device),
             torch.empty((n,), dtype=torch.float32, device=device),
-            torch.empty(sh.shape, dtype=sh.dtype, device=device))
+            torch.empty(acc_shape, dtype=torch.float32, device=device))
     fs.wait_event(after)
     done = torch.cuda.Event()
     with torch.cuda.stream(fs):

@@ -354,6 +354,39 @@ int gsx_render_forward_ordered(const gsx_raster_params *p, int64_t n, int64_t n_
                                const float *c2w, float *out, const int32_t *tile_order,
                                void *stream);
 
+/*
+ * Opt-in per-Gaussian colours (no reference counterpart: the reference
+ * evaluates SH per pixel, gs/src/include/vol_render_sh.h:139-141, 208-217).
+ * gsx_project_colors writes rgb f32[n,3] = sigmoid(sh . Y(dir)) with dir the
+ * unit vector from cam_pos (host float[3], the camera centre) to mean[i], the
+ * reference's SH basis and sigmoid colour; Gaussians with counts[i] <= 0
+ * (counts may be NULL) get 0.  gsx_project_colors_backward overwrites
+ * grad_sh f32[n,3,sh_stride] from grad_rgb f32[n,3] and ADDS the gradient
+ * through the direction into grad_mean f32[n,3] (so it runs after
+ * gsx_project_backward).  gsx_render_forward_rgb / gsx_render_backward_rgb
+ * composite those colours (no per-pixel SH; grad_rgb is added into, the caller
+ * zeroes it); tile_order may be NULL or as for the *_ordered entry points.
+ */
+int gsx_project_colors(int64_t n, const float *mean, const float *sh, int32_t sh_stride,
+                       int32_t sh_order, const float *cam_pos, const int32_t *counts, float *rgb,
+                       void *stream);
+int gsx_project_colors_backward(int64_t n, const float *mean, const float *sh, int32_t sh_stride,
+                                int32_t sh_order, const float *cam_pos, const int32_t *counts,
+                                const float *rgb, const float *grad_rgb, float *grad_sh,
+                                float *grad_mean, void *stream);
+int gsx_render_forward_rgb(const gsx_raster_params *p, int64_t n, int64_t n_keys,
+                           const float *mean2d, const float *cov2d, const float *rgb,
+                           const float *alpha, const int32_t *start, const int32_t *end,
+                           const int32_t *gaussian_ids, const float *topleft, const float *c2w,
+                           float *out, const int32_t *tile_order, void *stream);
+int gsx_render_backward_rgb(const gsx_raster_params *p, int64_t n, int64_t n_keys,
+                            const float *mean2d, const float *cov2d, const float *rgb,
+                            const float *alpha, const int32_t *start, const int32_t *end,
+                            const int32_t *gaussian_ids, const float *topleft, const float *c2w,
+                            const float *out, const float *grad_out, float *grad_mean2d,
+                            float *grad_cov2d, float *grad_rgb, float *grad_alpha,
+                            const int32_t *tile_order, void *stream);
+
 /* Backward raster; grad_* are added into (caller zeroes them). */
 int gsx_render_backward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
                         const float *mean2d, const float *cov2d, const float *sh,

@@ -147,7 +147,19 @@ def project(mean, qvec, log_scale, alpha_logit, cam: Cam64, st: Settings64, mode
 def sh_basis(cam: Cam64, px, py, C: int):
     c = cam.c2w
     d = torch.stack([c[3 * r] * px + c[3 * r + 1] * py + c[3 * r + 2] for r in range(3)], -1)
-    d = d / d.norm(dim=-1, keepdim=True)
+    return sh_basis_dir(d / d.norm(dim=-1, keepdim=True), C)
+
+
+def gaussian_colors(mean, sh, cam: Cam64, C: int):
+    """Per-Gaussian colours of the opt-in mode: sigmoid(sh . Y(dir)) with dir
+    the unit vector from the camera centre (c2w[:, 3]) to the mean; [..., N, 3]."""
+    d = mean - cam.c2w.reshape(3, 4)[:, 3]
+    Y = sh_basis_dir(d / d.norm(dim=-1, keepdim=True), C)           # [..., N, C*C]
+    return torch.sigmoid((sh[..., :C * C] * Y.unsqueeze(-2)).sum(-1))
+
+
+def sh_basis_dir(d, C: int):
+    """Real SH basis (shencoder.h:13-58) at unit directions d [..., 3]."""
     x, y, z = d.unbind(-1)
     Y = [torch.full_like(x, SH_C[0])]
     if C > 1:
@@ -172,11 +184,12 @@ def tile_pixels(cam: Cam64, st: Settings64, tx: int, ty: int, device):
     return GX, GY, px, py
 
 
-def composite(px, py, Y, mean2d, cov, opac, sh, member, T_thresh, extras: bool = False, z=None):
+def composite(px, py, Y, mean2d, cov, opac, sh, member, T_thresh, extras: bool = False, z=None, rgb=None):
     """Pixels [P] x depth-ordered Gaussians [..., M] -> colours [..., P, 3]
     (with extras: also the final transmittance [..., P] and the depth sum
     sum T a G z [..., P]).  member [..., M] masks Gaussians that are not on
-    this tile's list."""
+    this tile's list.  rgb [..., M, 3]: per-Gaussian colours instead of the
+    per-pixel SH colour."""
     dx = px.unsqueeze(-1) - mean2d[..., None, :, 0]
     dy = py.unsqueeze(-1) - mean2d[..., None, :, 1]
     c0, c1, c2, c3 = (cov[..., None, :, k] for k in range(4))
@@ -193,7 +206,10 @@ def composite(px, py, Y, mean2d, cov, opac, sh, member, T_thresh, extras: bool =
     T = torch.cat([torch.ones_like(Tin[..., :1]), Tin[..., :-1]], -1)
     inc = valid & (T >= T_thresh)
     wgt = torch.where(inc, T * eff, torch.zeros_like(eff))             # [..., P, M]
-    col = torch.sigmoid(torch.einsum("...mck,pk->...pmc", sh, Y))      # [..., P, M, 3]
+    if rgb is not None:
+        col = rgb.unsqueeze(-3)                                         # [..., 1, M, 3]
+    else:
+        col = torch.sigmoid(torch.einsum("...mck,pk->...pmc", sh, Y))  # [..., P, M, 3]
     rgb = (wgt.unsqueeze(-1) * col).sum(-2)
     if not extras:
         return rgb
@@ -203,12 +219,15 @@ def composite(px, py, Y, mean2d, cov, opac, sh, member, T_thresh, extras: bool =
 
 
 def render(mean, qvec, log_scale, sh, alpha_logit, cam: Cam64, st: Settings64, C: int, mode: str = "exact",
-           bg=None, maps: bool = False):
+           bg=None, maps: bool = False, sh_mode: str = "pixel"):
     """Full image [H, W, 3] (float64, differentiable); bg: background RGB
     composited behind (out += T_final bg); maps: also return the alpha map
-    (1 - T_final) and the depth map (sum T a G z), [H, W] each."""
+    (1 - T_final) and the depth map (sum T a G z), [H, W] each; sh_mode
+    "gaussian": one colour per Gaussian (gaussian_colors) instead of the
+    per-pixel SH colour."""
     dev = mean.device
     pr = project(mean, qvec, log_scale, alpha_logit, cam, st, mode)
+    rgb_all = gaussian_colors(mean, sh, cam, C) if sh_mode == "gaussian" else None
     img = torch.zeros((cam.h, cam.w, 3), dtype=F64, device=dev)
     Tmap = torch.ones((cam.h, cam.w), dtype=F64, device=dev)
     dmap = torch.zeros((cam.h, cam.w), dtype=F64, device=dev)
@@ -227,7 +246,8 @@ def render(mean, qvec, log_scale, sh, alpha_logit, cam: Cam64, st: Settings64, C
             Y = sh_basis(cam, px, py, C)
             c, Tf, ds = composite(px, py, Y, pr["mean2d"][idx], pr["cov"][idx], pr["opac"][idx], shc[idx],
                                   torch.ones(idx.numel(), dtype=torch.bool, device=dev), st.T_thresh,
-                                  extras=True, z=pr["depth"][idx])
+                                  extras=True, z=pr["depth"][idx],
+                                  rgb=rgb_all[idx] if rgb_all is not None else None)
             img = img.index_put((GY, GX), c)
             Tmap = Tmap.index_put((GY, GX), Tf)
             dmap = dmap.index_put((GY, GX), ds)
@@ -236,10 +256,10 @@ def render(mean, qvec, log_scale, sh, alpha_logit, cam: Cam64, st: Settings64, C
     return (img, 1.0 - Tmap, dmap) if maps else img
 
 
-def param_grads(params64, W, cam: Cam64, st: Settings64, C: int, mode: str, bg=None):
+def param_grads(params64, W, cam: Cam64, st: Settings64, C: int, mode: str, bg=None, sh_mode: str = "pixel"):
     """Autograd gradients of sum(W * image) in float64: dict of 5 tensors."""
     ps = [p.detach().clone().requires_grad_(True) for p in params64]
-    img = render(*ps, cam, st, C, mode, bg=bg)
+    img = render(*ps, cam, st, C, mode, bg=bg, sh_mode=sh_mode)
     (img * W).sum().backward()
     return dict(zip(["mean", "qvec", "log_scale", "sh", "alpha_logit"], [p.grad for p in ps])), img.detach()
 
