@@ -170,7 +170,7 @@ def run_gsx(args):
         dist.init_process_group("nccl", device_id=dev)
     wl = S.headline_workload(n=args.n) if args.workload == "headline" else S.small_workload()
     sc, view = wl.scene, wl.views[0]
-    settings = renderer.RasterSettings(tile_w=view.tile, tile_h=view.tile)
+    settings = renderer.RasterSettings(tile_w=view.tile, tile_h=view.tile, sh_mode=args.sh_mode)
     params = [torch.from_numpy(a).to(dev) for a in (sc.mean, sc.qvec, sc.log_scale, sc.sh, sc.alpha_logit)]
     W = torch.from_numpy(wl.grad_weight).to(dev)
     pipe = renderer.ViewPipeline(dev)
@@ -267,7 +267,8 @@ def run_gsx(args):
     P = view.cam.w * view.cam.h
     n_tiles = settings.tiles(view.cam)[0] * settings.tiles(view.cam)[1]
     dom = max(stages, key=lambda k: stages[k]["mean_ms"])
-    alg = algorithmic_bytes(dom, sc.n, K, P, sc.sh_order, n_tiles)
+    # per-Gaussian colours: the raster reads 3 floats of colour per key, as C = 1 would
+    alg = algorithmic_bytes(dom, sc.n, K, P, sc.sh_order if args.sh_mode == "pixel" else 1, n_tiles)
     achieved = alg / (stages[dom]["mean_ms"] * 1e-3) / 1e9
     peak = float(peaks["hbm_gbs"])
     line = {
@@ -300,13 +301,14 @@ def run_gsx(args):
         "gpu_launches": launches,
         "wall_s": round(wall1 - wall0, 3),
     }
-    prof = profiled_traffic(dom, args.workload) if args.n == 1_000_000 else None
+    captured = args.n == 1_000_000 and args.sh_mode == "pixel"  # the committed ncu captures cover this case
+    prof = profiled_traffic(dom, args.workload) if captured else None
     if prof is not None:
         line["roofline"]["traffic"] = prof[0]
         line["roofline"]["traffic_source"] = f"ncu dram__bytes_read.sum + dram__bytes_write.sum, {prof[1]}"
     line["roofline"]["note"] = ("raster kernels are FP32/SFU-issue bound (see profiles/); the HBM fraction "
                                 "counts each key's Gaussian record once per tile")
-    inst = profiled_traffic(dom, args.workload, "warp_inst_per_launch") if args.n == 1_000_000 else None
+    inst = profiled_traffic(dom, args.workload, "warp_inst_per_launch") if captured else None
     if inst is not None and clock_info.get("sm_mhz"):
         # the bound these kernels meet: one warp instruction per scheduler per
         # cycle (152 SMs x 4), at the SM clock sampled during the timed region
@@ -317,7 +319,10 @@ def run_gsx(args):
                                      "unit": "G warp-inst/s", "frac": round(got_issue / peak_issue, 4),
                                      "warp_inst_per_launch": inst[0], "source": f"ncu smsp__inst_executed.sum, "
                                                                                 f"{inst[1]}"}
-    if not args.no_cpu_baseline:
+    if args.sh_mode == "gaussian":  # the opt-in mode: not the reference's images, no CPU counterpart
+        line["metric"] += ", per-Gaussian SH colours"
+        line["config"]["sh_mode"] = "gaussian: one SH colour per Gaussian per view (opt-in, not the reference's images)"
+    elif not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(wl, args.cpu_frac)
     print(json.dumps(line), flush=True)
 
@@ -730,6 +735,8 @@ def main():
     ap.add_argument("--plain-requests", type=int, default=1000)
     ap.add_argument("--n-memory", type=int, default=3_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sh-mode", default="pixel", choices=["pixel", "gaussian"],
+                    help="headline: SH colour per pixel (the reference) or per Gaussian (opt-in)")
     ap.add_argument("--cpu-frac", type=float, default=1.0 / 8.0)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -80,6 +80,42 @@ __device__ __forceinline__ float view_dir(const float *m, float3 cam, float &dx,
   return len;
 }
 
+// One channel row of CC coefficients: 16-byte accesses when the row starts
+// on a 16-byte boundary and CC is a multiple of 4 (C = 2, 4 with such a
+// stride), else scalar ones.
+template <int CC>
+__device__ __forceinline__ void load_row(const float *__restrict__ p, bool vec, float (&v)[CC]) {
+  if constexpr (CC % 4 == 0) {
+    if (vec) {
+#pragma unroll
+      for (int k = 0; k < CC; k += 4) {
+        const float4 q = *reinterpret_cast<const float4 *>(p + k);
+        v[k] = q.x;
+        v[k + 1] = q.y;
+        v[k + 2] = q.z;
+        v[k + 3] = q.w;
+      }
+      return;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < CC; ++k) v[k] = p[k];
+}
+
+template <int CC>
+__device__ __forceinline__ void store_row(float *__restrict__ p, bool vec, const float (&v)[CC]) {
+  if constexpr (CC % 4 == 0) {
+    if (vec) {
+#pragma unroll
+      for (int k = 0; k < CC; k += 4)
+        *reinterpret_cast<float4 *>(p + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+      return;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < CC; ++k) p[k] = v[k];
+}
+
 template <int C>
 __global__ void __launch_bounds__(256)
     colors_forward_kernel(int64_t n, const float *__restrict__ mean, const float *__restrict__ sh,
@@ -97,12 +133,14 @@ __global__ void __launch_bounds__(256)
   view_dir(mean + 3 * g, cam, x, y, z);
   float Y[CC];
   sh_basis_dir<C, float>(x, y, z, Y);
+  const bool vec = ((sh_stride & 3) == 0) && ((reinterpret_cast<uintptr_t>(sh) & 15) == 0);
 #pragma unroll
   for (int ch = 0; ch < 3; ++ch) {
-    const float *s = sh + (g * 3 + ch) * sh_stride;
+    float v[CC];
+    load_row<CC>(sh + (g * 3 + ch) * sh_stride, vec, v);
     float logit = 0.0f;
 #pragma unroll
-    for (int k = 0; k < CC; ++k) logit = fmaf(s[k], Y[k], logit);
+    for (int k = 0; k < CC; ++k) logit = fmaf(v[k], Y[k], logit);
     o[ch] = gsx_sigmoidf(logit);
   }
 }
@@ -126,21 +164,25 @@ __global__ void __launch_bounds__(256)
   sh_basis_dir<C, D3>(D3{x, 1.0f, 0.0f, 0.0f}, D3{y, 0.0f, 1.0f, 0.0f}, D3{z, 0.0f, 0.0f, 1.0f},
                       Y);
   float gx = 0.0f, gy = 0.0f, gz = 0.0f;  // dL/ddir
+  const bool vec = ((sh_stride & 3) == 0) && ((reinterpret_cast<uintptr_t>(sh) & 15) == 0) &&
+                   ((reinterpret_cast<uintptr_t>(g_sh) & 15) == 0);
 #pragma unroll
   for (int ch = 0; ch < 3; ++ch) {
     const float c = rgb[3 * g + ch];
     const float dl = g_rgb[3 * g + ch] * (c * (1.0f - c));  // dL/dlogit
-    const float *s = sh + (g * 3 + ch) * sh_stride;
-    float *gs = g_sh + (g * 3 + ch) * sh_stride;
+    float v[CC], gs[CC];
+    load_row<CC>(sh + (g * 3 + ch) * sh_stride, vec, v);
 #pragma unroll
     for (int k = 0; k < CC; ++k) {
       gs[k] = dl * Y[k].v;
-      const float w = dl * s[k];
+      const float w = dl * v[k];
       gx = fmaf(w, Y[k].x, gx);
       gy = fmaf(w, Y[k].y, gy);
       gz = fmaf(w, Y[k].z, gz);
     }
-    for (int k = CC; k < sh_stride; ++k) gs[k] = 0.0f;
+    float *row = g_sh + (g * 3 + ch) * sh_stride;
+    store_row<CC>(row, vec, gs);
+    for (int k = CC; k < sh_stride; ++k) row[k] = 0.0f;
   }
   if (len > 0.0f) {  // d dir / d mean = (I - dir dir^T) / len
     const float dot = fmaf(z, gz, fmaf(y, gy, x * gx));
