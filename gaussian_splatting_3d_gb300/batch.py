@@ -105,6 +105,8 @@ class BatchPipeline:
         st = self.settings
         if st.bg is not None or st.output_maps:
             raise NotImplementedError("batched passes composite no background and write no maps")
+        if st.sh_mode != "pixel" or st.sh_dir != "reference":
+            raise NotImplementedError("batched passes use the reference's per-pixel SH colour")
         self.scenes = scenes
         self.views = views
         self.backward_enabled = backward

@@ -87,6 +87,11 @@ class RasterSettings:
     # centre -> mean, computed once in the projection (opt-in, not the
     # reference's images)
     sh_mode: str = "pixel"
+    # per-pixel SH direction: "reference" reads the [3,4] camera-to-world with
+    # a row stride of 3, as the reference does (vol_render_sh.h:48-65);
+    # "ray" uses the true ray direction R (x, y, 1) (opt-in, not the
+    # reference's images)
+    sh_dir: str = "reference"
 
     def grad_flags(self) -> int:
         if self.exact_grad:
@@ -235,12 +240,24 @@ def _raster_params(cam: CameraInfo, settings: RasterSettings, C: int, sh_stride:
     return p
 
 
-def camera_consts(c2w_np, cam: CameraInfo) -> torch.Tensor:
-    """Pinned host tensor [14]: the image-plane top-left corner (2 floats)
-    and the row-major [3,4] camera-to-world matrix the raster reads."""
+def camera_floats(c2w_np, cam: CameraInfo, sh_dir: str = "reference") -> np.ndarray:
+    """float32 [14]: the image-plane top-left corner (2 floats) and the 12
+    camera floats the raster reads for the per-pixel SH direction (rows of 3
+    at float offsets 0, 3, 6).  "reference": the row-major [3,4]
+    camera-to-world as is, so the direction uses its misread rows as the
+    reference does; "ray": the rotation's rows packed contiguously, so the
+    same reads give the ray direction R (x, y, 1)."""
+    if sh_dir not in ("reference", "ray"):
+        raise ValueError(f"sh_dir must be 'reference' or 'ray' (got {sh_dir!r})")
+    m = np.ascontiguousarray(c2w_np, dtype=np.float32).reshape(3, 4)
+    flat = m.reshape(12) if sh_dir == "reference" else np.concatenate([m[:, :3].reshape(9), m[:, 3]])
+    return np.concatenate([np.asarray(cam.topleft(), np.float32), flat]).astype(np.float32)
+
+
+def camera_consts(c2w_np, cam: CameraInfo, sh_dir: str = "reference") -> torch.Tensor:
+    """camera_floats in a pinned host tensor (uploaded without blocking)."""
     t = torch.empty(14, dtype=torch.float32, pin_memory=True)
-    t[:2] = torch.tensor(cam.topleft(), dtype=torch.float32)
-    t[2:] = torch.from_numpy(np.ascontiguousarray(c2w_np, dtype=np.float32).reshape(12))
+    t.copy_(torch.from_numpy(camera_floats(c2w_np, cam, sh_dir)))
     return t
 
 
@@ -283,7 +300,7 @@ class ViewPipeline:
             pr = project(mean, qvec, log_scale, alpha_logit, gcam, settings)
         ntw, nth = settings.tiles(cam)
         if cam_consts is None:
-            cam_consts = camera_consts(c2w_np, cam).to(dev, non_blocking=True)
+            cam_consts = camera_consts(c2w_np, cam, settings.sh_dir).to(dev, non_blocking=True)
         topleft, c2w_dev = cam_consts[:2], cam_consts[2:]
         out = torch.empty((cam.h, cam.w, 3), dtype=torch.float32, device=dev)
         order = torch.empty((ntw * nth,), dtype=torch.int32, device=dev)
@@ -540,7 +557,7 @@ class FusedRender(torch.autograd.Function):
             dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
             with torch.cuda.device(dev):
                 (mean, qvec, log_scale, sh, alpha_logit), cam_consts, sh_ready = _upload_overlapped(
-                    tensors, camera_consts(c2w_np, cam), dev)
+                    tensors, camera_consts(c2w_np, cam, settings.sh_dir), dev)
         else:
             for x, name in zip(tensors, names):
                 check_tensor(x, name)

@@ -144,9 +144,12 @@ def project(mean, qvec, log_scale, alpha_logit, cam: Cam64, st: Settings64, mode
     return dict(mean2d=mean2d, cov=cov, depth=p[..., 2], opac=opac, rect=rect, keep=keep)
 
 
-def sh_basis(cam: Cam64, px, py, C: int):
+def sh_basis(cam: Cam64, px, py, C: int, sh_dir: str = "reference"):
+    """Per-pixel SH basis; "reference": the direction from the flat c2w read
+    with a row stride of 3 (vol_render_sh.h:48-65); "ray": R (x, y, 1)."""
     c = cam.c2w
-    d = torch.stack([c[3 * r] * px + c[3 * r + 1] * py + c[3 * r + 2] for r in range(3)], -1)
+    s = 3 if sh_dir == "reference" else 4
+    d = torch.stack([c[s * r] * px + c[s * r + 1] * py + c[s * r + 2] for r in range(3)], -1)
     return sh_basis_dir(d / d.norm(dim=-1, keepdim=True), C)
 
 
@@ -219,7 +222,7 @@ def composite(px, py, Y, mean2d, cov, opac, sh, member, T_thresh, extras: bool =
 
 
 def render(mean, qvec, log_scale, sh, alpha_logit, cam: Cam64, st: Settings64, C: int, mode: str = "exact",
-           bg=None, maps: bool = False, sh_mode: str = "pixel"):
+           bg=None, maps: bool = False, sh_mode: str = "pixel", sh_dir: str = "reference"):
     """Full image [H, W, 3] (float64, differentiable); bg: background RGB
     composited behind (out += T_final bg); maps: also return the alpha map
     (1 - T_final) and the depth map (sum T a G z), [H, W] each; sh_mode
@@ -243,7 +246,7 @@ def render(mean, qvec, log_scale, sh, alpha_logit, cam: Cam64, st: Settings64, C
                 continue
             idx = idx[torch.argsort(pr["depth"].detach()[idx], stable=True)]
             GX, GY, px, py = tile_pixels(cam, st, tx, ty, dev)
-            Y = sh_basis(cam, px, py, C)
+            Y = sh_basis(cam, px, py, C, sh_dir)
             c, Tf, ds = composite(px, py, Y, pr["mean2d"][idx], pr["cov"][idx], pr["opac"][idx], shc[idx],
                                   torch.ones(idx.numel(), dtype=torch.bool, device=dev), st.T_thresh,
                                   extras=True, z=pr["depth"][idx],
@@ -256,10 +259,11 @@ def render(mean, qvec, log_scale, sh, alpha_logit, cam: Cam64, st: Settings64, C
     return (img, 1.0 - Tmap, dmap) if maps else img
 
 
-def param_grads(params64, W, cam: Cam64, st: Settings64, C: int, mode: str, bg=None, sh_mode: str = "pixel"):
+def param_grads(params64, W, cam: Cam64, st: Settings64, C: int, mode: str, bg=None, sh_mode: str = "pixel",
+                sh_dir: str = "reference"):
     """Autograd gradients of sum(W * image) in float64: dict of 5 tensors."""
     ps = [p.detach().clone().requires_grad_(True) for p in params64]
-    img = render(*ps, cam, st, C, mode, bg=bg, sh_mode=sh_mode)
+    img = render(*ps, cam, st, C, mode, bg=bg, sh_mode=sh_mode, sh_dir=sh_dir)
     (img * W).sum().backward()
     return dict(zip(["mean", "qvec", "log_scale", "sh", "alpha_logit"], [p.grad for p in ps])), img.detach()
 

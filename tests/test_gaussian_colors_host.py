@@ -58,3 +58,19 @@ def test_gaussian_mode_autograd_matches_finite_differences(mode):
             fd = (loss(plus) - loss(minus)) / (2 * h)
             if name == "sh" or mode == "exact":  # parity detaches depth and J, the colour path is exact
                 assert abs(fd - float(g[name][idx])) <= 1e-5 * max(1.0, abs(fd)), (name, idx, fd, float(g[name][idx]))
+
+
+def test_ray_direction_camera_constants():
+    """camera_floats(..., "ray") packs the rotation rows so that the raster's
+    stride-3 reads give R (x, y, 1); "reference" keeps the flat [3,4]."""
+    from gaussian_splatting_3d_gb300 import renderer
+    from gaussian_splatting_3d_gb300.camera import CameraInfo, look_at_c2w
+
+    cam = CameraInfo.from_vertical_fov(50.0, 64, 48)
+    c2w = look_at_c2w((1.0, -6.0, 2.0))
+    ref = renderer.camera_floats(c2w, cam, "reference")[2:]
+    ray = renderer.camera_floats(c2w, cam, "ray")[2:]
+    np.testing.assert_array_equal(ref, c2w.reshape(-1))
+    v = np.array([0.3, -0.2, 1.0], np.float32)
+    d = np.array([ray[3 * r] * v[0] + ray[3 * r + 1] * v[1] + ray[3 * r + 2] for r in range(3)])
+    np.testing.assert_allclose(d, c2w[:, :3] @ v, rtol=1e-6)

@@ -66,3 +66,27 @@ def test_gaussian_mode_differs_from_pixel_mode_and_is_cheaper_to_composite():
     hue = (a[lit] / a[lit].sum(-1, keepdim=True)).cpu().numpy()
     assert np.ptp(hue, axis=0).max() < 1e-5
     assert float((a - b).abs().max()) > 1e-4
+
+
+@pytest.mark.parametrize("mode", ["parity", "exact"])
+def test_true_ray_sh_direction_matches_fp64(mode):
+    """RasterSettings(sh_dir="ray"): the per-pixel SH direction is R (x, y, 1)
+    instead of the reference's stride-3 read of the flat c2w; image and
+    gradients equal the FP64 restatement of that direction."""
+    wl = S.custom_workload(3000, 96, 64, 3, seed=79)
+    sc, view = wl.scene, wl.views[0]
+    st = renderer.RasterSettings(sh_dir="ray", exact_grad=(mode == "exact"))
+    ps = [torch.from_numpy(a).to(dev()).requires_grad_(True) for a in
+          (sc.mean, sc.qvec, sc.log_scale, sc.sh, sc.alpha_logit)]
+    img = renderer.rasterize(*ps, view.c2w, view.cam, st)
+    W = torch.from_numpy(wl.grad_weight).to(dev())
+    (img * W).sum().backward()
+    cam = R.Cam64.from_view(view.c2w, view.cam, device=dev())
+    ref, img64 = R.param_grads(R.to64(sc, dev()), W.double(), cam, R.Settings64(), sc.sh_order, mode,
+                               sh_dir="ray")
+    assert float((img.detach().double() - img64).abs().max()) <= 4e-6
+    for k, p in zip(KEYS, ps):
+        e = rel_err(p.grad.double().cpu().numpy(), ref[k].cpu().numpy())
+        assert e <= GRAD_REL, f"{mode} {k}: {e:.3g}"
+    ref_img = renderer.rasterize(*[p.detach() for p in ps], view.c2w, view.cam, renderer.RasterSettings())
+    assert float((img.detach() - ref_img).abs().max()) > 1e-4  # a different image from the reference's
