@@ -229,11 +229,13 @@ def run_gsx(args):
 
     def e2e_step():
         ps = [h.detach().requires_grad_(True) for h in host]
-        side.wait_stream(main)
-        with torch.cuda.stream(side):
-            w = Wh.to(dev, non_blocking=True)
         img = renderer.rasterize(*ps, view.c2w, view.cam, settings, device=dev)
-        main.wait_stream(side)
+        # the loss weights follow the parameters on the upload stream: they
+        # are needed only by the backward, the SH coefficients by the forward
+        up = renderer.copy_stream(dev)
+        with torch.cuda.stream(up):
+            w = Wh.to(dev, non_blocking=True)
+        main.wait_stream(up)
         w.record_stream(main)
         side.wait_stream(main)
         with torch.cuda.stream(side):

@@ -377,7 +377,7 @@ class ViewPipeline:
             st["grads"], st["grads_ready"] = grads, grads_ready
         return st
 
-    def backward(self, state, mean, qvec, log_scale, sh, alpha_logit, grad_out, timer=None):
+    def backward(self, state, mean, qvec, log_scale, sh, alpha_logit, grad_out, timer=None, sh_grad_sink=None):
         dev = mean.device
         n = mean.shape[0]
         pr = state["pr"]
@@ -407,6 +407,8 @@ class ViewPipeline:
                 _lib.call("gsx_render_backward_ordered", *common, ptr(state["order"]), stream_handle(dev))
             else:
                 _lib.call("gsx_render_backward", *common, stream_handle(dev))
+        if sh_grad_sink is not None and rgb is None:
+            sh_grad_sink(g_acc)  # dL/dsh is final here: the projection backward does not touch it
         g_mean = torch.empty_like(mean)
         g_q = torch.empty_like(qvec)
         g_ls = torch.empty_like(log_scale)
@@ -506,11 +508,27 @@ def _zeroed_grad_buffers(device, n: int, acc_shape: tuple, after: torch.cuda.Eve
     return bufs, done
 
 
-def _copy_stream(device) -> torch.cuda.Stream:
+def copy_stream(device) -> torch.cuda.Stream:
+    """The stream on which host-resident ``rasterize`` uploads the parameters
+    of `device`.  A caller's further host->device copies for the same step
+    (e.g. the loss weights) enqueued here after the call land behind the
+    parameters instead of sharing the link with them, so the SH coefficients
+    the raster waits for arrive first."""
+    device = torch.device(device)
     key = (device.type, device.index)
     if key not in _copy_streams:
         _copy_streams[key] = torch.cuda.Stream(device)
     return _copy_streams[key]
+
+
+_d2h_streams: dict = {}
+
+
+def _d2h_stream(device) -> torch.cuda.Stream:
+    key = (device.type, device.index)
+    if key not in _d2h_streams:
+        _d2h_streams[key] = torch.cuda.Stream(device)
+    return _d2h_streams[key]
 
 
 def _upload_overlapped(host, consts, device):
@@ -523,7 +541,7 @@ def _upload_overlapped(host, consts, device):
     current stream queues behind them.  Returns the device tensors, the
     device constants and the event the raster stage must wait for."""
     main = torch.cuda.current_stream(device)
-    cs = _copy_stream(device)
+    cs = copy_stream(device)
     dev_t = [torch.empty(h.shape, dtype=h.dtype, device=device) for h in host]
     dev_c = torch.empty(consts.shape, dtype=consts.dtype, device=device)
     cs.wait_stream(main)  # the fresh buffers may reuse memory the main stream still reads
@@ -579,14 +597,40 @@ class FusedRender(torch.autograd.Function):
     @staticmethod
     def backward(ctx, grad_out):
         mean, qvec, log_scale, sh, alpha_logit = ctx.saved_tensors
-        with torch.cuda.device(mean.device):
-            grads = ctx.pipe.backward(ctx.state, mean, qvec, log_scale, sh, alpha_logit, grad_out)
-            if ctx.host_mode:  # gradients of host parameters live on the host
-                host = tuple(torch.empty(g.shape, dtype=g.dtype, pin_memory=True) for g in grads)
-                for h, g in zip(host, grads):
+        dev = mean.device
+        with torch.cuda.device(dev):
+            if not ctx.host_mode:
+                grads = ctx.pipe.backward(ctx.state, mean, qvec, log_scale, sh, alpha_logit, grad_out)
+            else:
+                # gradients of host parameters live on the host.  dL/dsh (the
+                # bulk of the bytes) starts its download on a side stream as
+                # soon as the raster backward has produced it, overlapping the
+                # projection backward; the other four follow.
+                main = torch.cuda.current_stream(dev)
+                d2h = _d2h_stream(dev)
+                sh_host = []
+
+                def sink(g):
+                    h = torch.empty(g.shape, dtype=g.dtype, pin_memory=True)
+                    d2h.wait_stream(main)
+                    with torch.cuda.stream(d2h):
+                        h.copy_(g, non_blocking=True)
+                    g.record_stream(d2h)
+                    sh_host.append(h)
+
+                grads = ctx.pipe.backward(ctx.state, mean, qvec, log_scale, sh, alpha_logit, grad_out,
+                                          sh_grad_sink=sink)
+                host = []
+                for k, g in enumerate(grads):
+                    if k == 3 and sh_host:
+                        host.append(sh_host[0])
+                        continue
+                    h = torch.empty(g.shape, dtype=g.dtype, pin_memory=True)
                     h.copy_(g, non_blocking=True)
-                torch.cuda.current_stream(mean.device).synchronize()
-                grads = host
+                    host.append(h)
+                main.synchronize()
+                d2h.synchronize()
+                grads = tuple(host)
         if ctx.aux is not None:
             ctx.aux["mean2d_grad"] = ctx.state["g_mean2d"]
         ctx.state = None
