@@ -59,6 +59,28 @@ def profiled_traffic(kernel: str, workload: str, what: str = "traffic_bytes_per_
     return None
 
 
+def host_link_gbs(pinned: torch.Tensor, dev, reps: int = 5) -> dict:
+    """Host<->device copy bandwidth (GB/s) of one pinned tensor, median of
+    `reps` copies each way timed with CUDA events."""
+    import torch
+
+    d = torch.empty(pinned.shape, dtype=pinned.dtype, device=dev)
+    back = torch.empty_like(pinned).pin_memory()
+    out = {}
+    for name, dst, src in (("h2d", d, pinned), ("d2h", back, d)):
+        ts = []
+        for _ in range(reps + 1):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            dst.copy_(src, non_blocking=True)
+            b.record()
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        out[name] = round(pinned.numel() * pinned.element_size() / (float(np.median(ts[1:])) * 1e-3) / 1e9, 1)
+    return out
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -262,6 +284,7 @@ def run_gsx(args):
         assert g is not None and not g.is_cuda and g.shape == h.shape
     h2d = sum(h.numel() * 4 for h in host) + Wh.numel() * 4
     d2h = sum(g.numel() * 4 for g in e2e_grads) + img_host.numel() * 4 + 4
+    link = host_link_gbs(host[3], dev)
 
     if rank != 0:
         return
@@ -295,7 +318,12 @@ def run_gsx(args):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "stages_ms": {k: round(v["mean_ms"], 4) for k, v in stages.items()},
         "e2e": {"value": round(e2e_ms, 4), "unit": "ms/iter", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
+                "d2h_bytes_per_step": int(d2h),
+                # the host link measured on this machine with one pinned copy of
+                # the SH coefficients each way; the step's bytes over it are
+                # the copy time the e2e figure cannot hide
+                "link_gbs": link,
+                "link_ms_per_step": round((h2d / link["h2d"] + d2h / link["d2h"]) / 1e6, 4)},
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 2), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
                      "peak_source": f"{peaks_kind} hbm_gbs", "algorithmic_bytes": int(alg)},

@@ -216,6 +216,28 @@ def binning_status(dev, n: int, capacity: int, n_tiles_w: int, n_tiles_h: int):
     return st, int(k.value)
 
 
+def binning_status_async(dev, n: int, capacity: int, block: torch.Tensor) -> torch.cuda.Event:
+    """Enqueue on the current stream a copy of the last binning's 16-byte
+    status block into `block` (16 bytes of pinned host memory) and return an
+    event: after event.synchronize(), decode_binning_status(block, ...) gives
+    what binning_status would.  Work enqueued after this call does not delay
+    the event, so a caller can launch the raster first and wait only for the
+    binning."""
+    buf = _bin_buffers(dev)
+    _lib.check(_lib.load().gsx_binning_status_copy_async(ptr(buf.ws), n, capacity, block.data_ptr(),
+                                                         stream_handle(dev)), "gsx_binning_status_copy_async")
+    ev = torch.cuda.Event()
+    ev.record(torch.cuda.current_stream(dev))
+    return ev
+
+
+def decode_binning_status(block: torch.Tensor, capacity: int, n_tiles_w: int, n_tiles_h: int):
+    """(status, key count) from a status block that has arrived."""
+    k = ctypes.c_int64(0)
+    st = _lib.load().gsx_binning_status_decode(block.data_ptr(), capacity, n_tiles_w, n_tiles_h, ctypes.byref(k))
+    return st, int(k.value)
+
+
 def raster_status(dev=None, clear: bool = True) -> int:
     """Sticky error bits of the raster kernels on `dev` (synchronises; 0 =
     no error).  Bit 0: a wait for the bulk copies of a batch's SH rows gave
@@ -273,6 +295,7 @@ class ViewPipeline:
     def __init__(self, device=None):
         self.device = torch.device(device or "cuda")
         self.key_capacity = 0  # grows to ~1.25x the largest key count seen
+        self.status_block = None  # pinned 16 bytes: the binning's status, read without a stream sync
 
     def forward(self, mean, qvec, log_scale, sh, alpha_logit, c2w_np, cam: CameraInfo,
                 settings: RasterSettings, timer=None, sh_ready=None, cam_consts=None,
@@ -313,6 +336,11 @@ class ViewPipeline:
         for _ in range(3):
             with ev("binning"):
                 ids, start, end = bin_gaussians_async(pr, ntw, nth, cap)
+            # the key count comes back without waiting for the raster enqueued
+            # below, so this call returns while the raster forward runs
+            if self.status_block is None:
+                self.status_block = torch.zeros(16, dtype=torch.uint8, pin_memory=True)
+            status_ev = binning_status_async(dev, n, cap, self.status_block)
             if want_grads and grads is None:
                 binned = torch.cuda.Event()
                 binned.record(torch.cuda.current_stream(dev))
@@ -349,7 +377,8 @@ class ViewPipeline:
                 # set up after the raster launch (host time off the GPU's critical path); the
                 # fill itself starts after the binning, whose working set lives in L2
                 grads, grads_ready = _zeroed_grad_buffers(dev, n, (n, 3) if rgb_mode else tuple(sh.shape), binned)
-            st, K = binning_status(dev, n, cap, ntw, nth)
+            status_ev.synchronize()
+            st, K = decode_binning_status(self.status_block, cap, ntw, nth)
             if st == _lib.GSX_ERR_CAPACITY:
                 cap = int(K * 1.25) + 4096
                 self.key_capacity = cap
