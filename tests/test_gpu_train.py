@@ -24,7 +24,7 @@ def dev():
 
 @pytest.mark.parametrize("loss_fn", ["l1", "l2"])
 @pytest.mark.parametrize("win", [11, 7])
-@pytest.mark.parametrize("hw", [(48, 64), (135, 240)])
+@pytest.mark.parametrize("hw", [(48, 64), (135, 240), (271, 481)])
 def test_photometric_loss_matches_fp64(loss_fn, win, hw):
     g = torch.Generator().manual_seed(1000 * win + hw[0] + (loss_fn == "l2"))
     H, W = hw
@@ -42,6 +42,22 @@ def test_photometric_loss_matches_fp64(loss_fn, win, hw):
     assert err <= 1e-4, err
 
 
+@pytest.mark.parametrize("hw,win", [((1, 4000), 1), ((2, 3000), 3), ((6, 1920), 11)])
+def test_photometric_loss_thin_images(hw, win):
+    """Fewer partial-sum slots than 32x32 tiles: a CTA walks several tiles."""
+    g = torch.Generator().manual_seed(hw[1] + win)
+    out = torch.rand(*hw, 3, generator=g)
+    gt = torch.rand(*hw, 3, generator=g)
+    st = train.LossSettings(ssim_mult=0.2, win_size=win, loss_fn="l2")
+    loss, grad = train.photometric_loss_with_grad(out.to(dev()), gt.to(dev()), st)
+    o64 = out.double().requires_grad_(True)
+    ref = L.photometric_loss(o64, gt.double(), 0.2, win, "l2")
+    ref.backward()
+    assert abs(float(loss) - float(ref.detach())) <= 1e-5 * abs(float(ref.detach()))
+    r = o64.grad.numpy()
+    assert np.abs(grad.cpu().double().numpy() - r).max() / np.abs(r).max() <= 1e-4
+
+
 def test_photometric_loss_autograd_feeds_renderer_gradient():
     g = torch.Generator().manual_seed(3)
     out = torch.rand(40, 50, 3, generator=g).to(dev()).requires_grad_(True)
@@ -54,7 +70,8 @@ def test_photometric_loss_autograd_feeds_renderer_gradient():
 
 def test_fused_adam_matches_torch_adam():
     g = torch.Generator().manual_seed(4)
-    shapes = [(1000, 3), (1000, 4), (1000, 3), (1000, 3, 16), (1000,)]
+    # sizes off the 4-element vectors and the 1024-element blocks
+    shapes = [(1000, 3), (1001, 4), (333, 3), (1000, 3, 16), (7,)]
     lrs = [1e-3, 1e-2, 1e-2, 1e-2, 1e-2]
     a = [torch.randn(s, generator=g).to(dev()) for s in shapes]
     b = [t.clone() for t in a]
@@ -71,3 +88,24 @@ def test_fused_adam_matches_torch_adam():
         opt_b.step()
         for p, q in zip(pa, pb):
             torch.testing.assert_close(p.data, q.data, rtol=1e-6, atol=1e-7)
+
+
+def test_fused_adam_many_groups():
+    """More groups than one warp scans at a time (the kernel's group search)."""
+    g = torch.Generator().manual_seed(5)
+    sizes = [int(s) for s in torch.randint(1, 3000, (70,), generator=g)]
+    a = [torch.randn(n, generator=g).to(dev()) for n in sizes]
+    pa = [torch.nn.Parameter(t) for t in a]
+    pb = [torch.nn.Parameter(t.clone()) for t in a]
+    lrs = [1e-3 * (1 + i % 7) for i in range(len(sizes))]
+    opt_a = train.FusedAdam([{"params": [p], "lr": lr} for p, lr in zip(pa, lrs)], betas=(0.9, 0.99))
+    opt_b = torch.optim.Adam([{"params": [p], "lr": lr} for p, lr in zip(pb, lrs)], betas=(0.9, 0.99))
+    for _ in range(2):
+        for p, q in zip(pa, pb):
+            gr = torch.randn(p.shape, generator=g).to(dev())
+            p.grad = gr.clone()
+            q.grad = gr.clone()
+        opt_a.step()
+        opt_b.step()
+    for p, q in zip(pa, pb):
+        torch.testing.assert_close(p.data, q.data, rtol=1e-6, atol=1e-7)
