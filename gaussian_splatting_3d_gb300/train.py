@@ -2,8 +2,8 @@
 
 ``photometric_loss(out, gt)`` is the reference's loss (utils/loss.py:5-24):
 ``ssim_mult * SSIM_loss + (1 - ssim_mult) * L2`` (or L1), with kornia's SSIM
-(Gaussian window, sigma 1.5, reflected borders); one native pass computes the
-loss and dL/dout, which the autograd backward hands to the renderer.
+(Gaussian window, sigma 1.5, reflected borders); two tiled native passes compute
+the loss and dL/dout, which the autograd backward hands to the renderer.
 
 ``FusedAdam`` is torch.optim.Adam as the reference builds it
 (gs/sh_renderer.py:720-729: one group per parameter tensor with its own
