@@ -1,0 +1,137 @@
+"""The bench's workload at its full size: 1,000,000 Gaussians, SH degree 3,
+1920x1080, 16x16 tiles (~4.2 M keys).
+
+* projection: bit-exact against the oracle for every Gaussian (as in the
+  small-case parity tests);
+* binning: the lists equal the oracle's bit for bit, and hold the
+  size-independent properties of the reference's sorted (tile, depth) keys:
+  the tile ranges partition [0, K) in tile order, every key's Gaussian
+  covers its tile, each tile's list ascends in depth bits with equal depths
+  in index order, and Gaussian g appears counts[g] times;
+* raster forward: every 8th row of tiles equals the oracle's within 4e-6
+  (the small cases hold 2e-6; here a pixel composites longer lists, each
+  term's colour a few ulp off the oracle's through the hardware sigmoid),
+  pixels the oracle leaves black stay black, and a second forward is
+  bit-identical;
+* backward: a second backward agrees within 1e-5 * max |g| per tensor (only
+  the order of float atomics differs).
+
+The file name sorts last so that the larger scene is drawn after the other
+GPU tests.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from gaussian_splatting_3d_gb300 import renderer, scene as S  # noqa: E402
+from gaussian_splatting_3d_gb300.camera import frustum_np, make_gsx_camera  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("raster_flags_clean")]
+
+IMG_ATOL = 4e-6
+ROW_STEP = 8
+
+
+def check_lists(ids, start, end, K, rect, depth, counts, n_tiles_w):
+    """Size-independent properties of tile lists sorted by (tile, depth bits,
+    index); raises AssertionError on the first violation."""
+    ids = np.asarray(ids)[:K].astype(np.int64)
+    start, end = np.asarray(start), np.asarray(end)
+    assert K == int(np.asarray(counts, np.int64).sum())
+    nonempty = start >= 0
+    assert np.array_equal(nonempty, end >= 0)
+    tiles = np.nonzero(nonempty)[0]
+    lens = (end - start)[tiles]
+    assert np.all(lens > 0) and int(lens.sum()) == K
+    assert start[tiles[0]] == 0 and end[tiles[-1]] == K
+    assert np.array_equal(start[tiles[1:]], end[tiles[:-1]])  # ranges in tile order, no gaps
+    tile_of_key = np.repeat(tiles, lens)
+    tx, ty = tile_of_key % n_tiles_w, tile_of_key // n_tiles_w
+    r = np.asarray(rect)[ids]
+    assert np.all((r[:, 0] <= tx) & (tx <= r[:, 2]) & (r[:, 1] <= ty) & (ty <= r[:, 3]))
+    key = (tile_of_key.astype(np.uint64) << np.uint64(32)) | \
+        np.asarray(depth, np.float32).view(np.uint32)[ids].astype(np.uint64)
+    up = key[1:] > key[:-1]
+    tie = (key[1:] == key[:-1]) & (ids[1:] > ids[:-1])
+    assert np.all(up | tie)
+    assert np.array_equal(np.bincount(ids, minlength=len(counts)), np.asarray(counts, np.int64))
+
+
+@pytest.fixture(scope="module")
+def headline():
+    wl = S.headline_workload()
+    sc, view = wl.scene, wl.views[0]
+    st = renderer.RasterSettings(tile_w=view.tile, tile_h=view.tile)
+    dev = torch.device("cuda:0")
+    params = [torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+              for a in (sc.mean, sc.qvec, sc.log_scale, sc.sh, sc.alpha_logit)]
+    cam = view.cam
+    normals, pts = frustum_np(view.c2w, cam)
+    ocam = O.make_camera(view.c2w, cam.fx, cam.fy, cam.cx, cam.cy, cam.w, cam.h, normals, pts)
+    opr = O.project(sc.mean, sc.qvec, sc.log_scale, sc.alpha_logit, ocam, 1.0, 6.0, view.tile, view.tile)
+    ntw, nth = st.tiles(cam)
+    ob = O.bin_gaussians(opr["rect"], opr["rect"][:, 2:], opr["depth"], nth, ntw, stride=4)
+    return dict(wl=wl, st=st, params=params, opr=opr, ob=ob, ntw=ntw, nth=nth)
+
+
+def test_headline_projection_and_lists(headline):
+    h = headline
+    wl, st, params, opr, ob = h["wl"], h["st"], h["params"], h["opr"], h["ob"]
+    view = wl.views[0]
+    pr = renderer.project(params[0], params[1], params[2], params[4], make_gsx_camera(view.c2w, view.cam), st)
+    counts = pr.counts.cpu().numpy()
+    vis = opr["mask"].astype(bool)
+    np.testing.assert_array_equal(counts, opr["counts"])
+    for k in ("rect", "mean2d", "cov2d", "depth"):
+        np.testing.assert_array_equal(getattr(pr, k).cpu().numpy()[vis], opr[k][vis], err_msg=k)
+    np.testing.assert_array_equal(pr.alpha.cpu().numpy(), opr["alpha"])
+    ids, start, end, K = renderer.bin_gaussians(pr, h["ntw"], h["nth"])
+    assert K > 1_000_000
+    ids, start, end = ids.cpu().numpy(), start.cpu().numpy(), end.cpu().numpy()
+    check_lists(ids, start, end, K, pr.rect.cpu().numpy(), pr.depth.cpu().numpy(), counts, h["ntw"])
+    assert K == ob["K"]
+    np.testing.assert_array_equal(ids[:K], ob["ids"])
+    np.testing.assert_array_equal(start, ob["start"])
+    np.testing.assert_array_equal(end, ob["end"])
+
+
+def test_headline_forward_rows_match_oracle_and_repeat(headline):
+    h = headline
+    wl, st, params, opr, ob = h["wl"], h["st"], h["params"], h["opr"], h["ob"]
+    sc, view = wl.scene, wl.views[0]
+    cam = view.cam
+    img = renderer.rasterize(*params, view.c2w, cam, st).cpu().numpy()
+    img2 = renderer.rasterize(*params, view.c2w, cam, st).cpu().numpy()
+    np.testing.assert_array_equal(img, img2)
+    ntw, nth = h["ntw"], h["nth"]
+    rows = np.arange(nth) % ROW_STEP == 0
+    start = ob["start"].reshape(nth, ntw).copy()
+    end = ob["end"].reshape(nth, ntw).copy()
+    start[~rows] = -1
+    end[~rows] = -1
+    P = O.raster_params(cam.w, cam.h, view.tile, view.tile, sc.sh_order, sc.sh.shape[-1])
+    ref = O.render_fwd(P, opr["mean2d"], opr["cov2d"], sc.sh, opr["alpha"], start.reshape(-1), end.reshape(-1),
+                       ob["ids"], np.array(cam.topleft(), np.float32), view.c2w, np.float32(1 / cam.fx),
+                       np.float32(1 / cam.fy))
+    pix_rows = np.repeat(rows, view.tile)[:cam.h]
+    got, want = img[pix_rows], ref[pix_rows]
+    d = np.abs(got.astype(np.float64) - want.astype(np.float64))
+    assert d.max() <= IMG_ATOL, f"image max |d| = {d.max():.3g}"
+    assert np.all(got[want == 0] == 0)
+
+
+def test_headline_backward_repeats(headline):
+    h = headline
+    wl, st = h["wl"], h["st"]
+    view = wl.views[0]
+    W = torch.from_numpy(wl.grad_weight).to("cuda:0")
+    runs = []
+    for _ in range(2):
+        ps = [p.clone().requires_grad_(True) for p in h["params"]]
+        (renderer.rasterize(*ps, view.c2w, view.cam, st) * W).sum().backward()
+        runs.append([p.grad.cpu().numpy().astype(np.float64) for p in ps])
+    for name, a, b in zip(("mean", "qvec", "log_scale", "sh", "alpha_logit"), *runs):
+        scale = max(np.abs(b).max(), 1e-3)
+        assert np.abs(a - b).max() <= 1e-5 * scale, name
