@@ -181,6 +181,9 @@ def cases():
     out.append(("c2_2k_64", S.custom_workload(2000, 64, 64, 1, seed=1), None))
     out.append(("c4_3k_100x75", S.custom_workload(3000, 100, 75, 3, seed=2), None))
     out.append(("c4_nowC2_1500_80x48", S.custom_workload(1500, 80, 48, 3, seed=4), 2))
+    # SH degree 2 (C = 3: nine coefficients per channel, the odd row length)
+    # on an image that is not a multiple of the tile
+    out.append(("c3_2500_90x70", S.custom_workload(2500, 90, 70, 2, seed=7), None))
     # equal keys: 60 copies of one Gaussian plus its neighbours at one depth
     base = S.custom_workload(1, 64, 48, 1, seed=11, radius=3.0)
     n = 60
