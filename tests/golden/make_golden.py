@@ -184,6 +184,8 @@ def cases():
     # SH degree 2 (C = 3: nine coefficients per channel, the odd row length)
     # on an image that is not a multiple of the tile
     out.append(("c3_2500_90x70", S.custom_workload(2500, 90, 70, 2, seed=7), None))
+    # longer tile lists: 8,000 larger Gaussians, SH degree 3, 200x150
+    out.append(("c4_8k_200x150", S.custom_workload(8000, 200, 150, 3, seed=8, log_scale_mu=-2.6), None))
     # equal keys: 60 copies of one Gaussian plus its neighbours at one depth
     base = S.custom_workload(1, 64, 48, 1, seed=11, radius=3.0)
     n = 60
