@@ -194,7 +194,9 @@ def bin_gaussians(pr: Projected, n_tiles_w: int, n_tiles_h: int, key_hint: int |
 
 def bin_gaussians_async(pr: Projected, n_tiles_w: int, n_tiles_h: int, capacity: int):
     """Enqueue the binning without synchronising: returns (ids[capacity],
-    start, end); binning_status() later gives the key count."""
+    start, end); binning_status() later gives the key count (it synchronises
+    the stream), or binning_status_async() + decode_binning_status() without
+    waiting for work enqueued after the binning."""
     n = pr.counts.shape[0]
     dev = pr.counts.device
     T = n_tiles_w * n_tiles_h
