@@ -88,3 +88,35 @@ def test_ordered_raster_entry_points_validate_on_the_host():
     assert lib.gsx_tile_order(None, None, -1, None, None) == _lib.GSX_ERR_INVALID_ARG
     assert lib.gsx_tile_order(None, None, 0, None, None) == _lib.GSX_OK
     assert lib.gsx_tile_order(None, None, 4, None, None) == _lib.GSX_ERR_INVALID_ARG
+
+
+def declared_arities():
+    """{name: parameter count} of every function declared in gsx.h."""
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    out = {}
+    for name, params in re.findall(r"\b(gsx_[a-z0-9_]+)\s*\(([^;{}]*?)\)\s*;", text, flags=re.S):
+        params = params.strip()
+        out[name] = 0 if params in ("", "void") else len(params.split(","))
+    return out
+
+
+def test_ctypes_table_matches_header_arity():
+    arity = declared_arities()
+    assert len(arity) >= 12
+    wrong = {n: (k, len(_lib.SIGNATURES[n][1])) for n, k in arity.items()
+             if n in _lib.SIGNATURES and len(_lib.SIGNATURES[n][1]) != k}
+    assert not wrong, f"(header, ctypes) parameter counts differ: {wrong}"
+
+
+def test_training_entry_points_validate_on_the_host():
+    lib = _lib.load()
+    assert lib.gsx_photometric_loss_workspace_bytes(1080, 1920) == 9 * 1080 * 1920 * 4
+    assert lib.gsx_photometric_loss_blocks(1080, 1920) == (3 * 1080 * 1920 + 255) // 256
+    ws = ctypes.c_void_p(1)  # never dereferenced: validation fails first
+    for win, h, w in ((4, 64, 64), (33, 64, 64), (11, 5, 64), (11, 64, 5)):
+        st = lib.gsx_photometric_loss(ws, ws, h, w, win, ctypes.c_float(0.2), 1, ws, None, ws,
+                                      1 << 30, None)
+        assert st == _lib.GSX_ERR_INVALID_ARG, (win, h, w)
+    assert lib.gsx_adam_step(None, None, 1, 10, None) == _lib.GSX_ERR_INVALID_ARG
+    assert lib.gsx_adam_step(ws, ws, 0, 10, None) == _lib.GSX_ERR_INVALID_ARG
