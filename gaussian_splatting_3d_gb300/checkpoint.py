@@ -5,9 +5,14 @@ dict of the five parameter tensors (``mean``, ``qvec``,
 ``svec_before_activation``, ``sh_coeffs``, ``alpha_before_activation``), the
 Gaussian count ``N`` and the training configuration ``cfg`` -- a Hydra /
 OmegaConf object in the reference's training runs.  Unpickling that object
-needs omegaconf, which a serving host need not have, so ``load_state`` maps
-classes whose module cannot be imported to inert stand-ins (the configuration
-is metadata here; the tensors are what is served).
+needs omegaconf, which a serving host need not have, and a pickle can name
+any importable callable, which unpickling would run.  So ``load_state``
+resolves only the names a tensor checkpoint needs (torch's tensor and storage
+rebuild functions, storage classes, ``torch.Size``, dtypes, builtin
+containers) and maps every other class -- omegaconf's included -- to an inert
+stand-in that keeps its pickled state (the configuration is metadata here;
+the tensors are what is served).  Nothing a checkpoint names beyond that
+list is imported or called.
 """
 from __future__ import annotations
 
@@ -33,12 +38,32 @@ class Opaque:
         return (type(self), self.__dict__.get("_args", ()), self.__dict__.get("_state"))
 
 
+_BUILTINS = {"dict", "list", "tuple", "set", "frozenset", "bytearray", "bytes", "str", "int", "float", "bool",
+             "complex", "slice", "range"}
+
+
+def _allowed(module: str, name: str) -> bool:
+    """Names a torch.save checkpoint of tensors needs to be rebuilt."""
+    if module == "torch._utils":
+        return name.startswith("_rebuild_")
+    if module == "torch":
+        return name.endswith("Storage") or name == "Size" or isinstance(getattr(torch, name, None), torch.dtype)
+    if module == "torch.storage":
+        return name in ("TypedStorage", "UntypedStorage")
+    if module == "collections":
+        return name == "OrderedDict"
+    if module == "builtins":
+        return name in _BUILTINS
+    if module == "_codecs":
+        return name == "encode"  # bytes objects pickled with protocol 2
+    return False
+
+
 class _Unpickler(pickle.Unpickler):
     def find_class(self, module, name):
-        try:
+        if _allowed(module, name):
             return super().find_class(module, name)
-        except (ImportError, AttributeError):
-            return type(name, (Opaque,), {"__module__": "gsx_missing." + module})
+        return type(name, (Opaque,), {"__module__": "gsx_missing." + module})
 
 
 class _PickleModule:

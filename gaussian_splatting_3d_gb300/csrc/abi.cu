@@ -30,6 +30,8 @@ int cuda_status(cudaError_t e, const char *what) {
   return GSX_ERR_CUDA;
 }
 
+void clear_error() { g_err[0] = 0; }
+
 }  // namespace gsx
 
 using namespace gsx;
@@ -43,6 +45,17 @@ using namespace gsx;
   } while (0)
 
 static inline cudaStream_t as_stream(void *s) { return static_cast<cudaStream_t>(s); }
+
+namespace gsx {
+int check_binning_sizes(int64_t n, int64_t cap, int32_t nth, int32_t ntw) {
+  GSX_REQUIRE(n >= 0 && n < (1ll << 30), "n must be in [0, 2^30) (got %lld)", (long long)n);
+  GSX_REQUIRE(cap >= 0 && cap < (1ll << 30), "key count must be in [0, 2^30) (got %lld)",
+              (long long)cap);
+  GSX_REQUIRE(nth > 0 && ntw > 0, "tile grid must be positive (got %d x %d)", ntw, nth);
+  GSX_REQUIRE((int64_t)nth * ntw < (1ll << 31), "too many tiles");
+  return GSX_OK;
+}
+}  // namespace gsx
 
 extern "C" {
 
@@ -80,15 +93,6 @@ size_t gsx_binning_workspace_bytes(int64_t n_gaussians, int64_t key_capacity,
                                    int64_t n_tiles) {
   if (n_gaussians < 0 || key_capacity < 0 || n_tiles < 0) return 0;
   return binning_workspace_bytes(n_gaussians, key_capacity, n_tiles);
-}
-
-static int check_binning_sizes(int64_t n, int64_t cap, int32_t nth, int32_t ntw) {
-  GSX_REQUIRE(n >= 0 && n < (1ll << 30), "n must be in [0, 2^30) (got %lld)", (long long)n);
-  GSX_REQUIRE(cap >= 0 && cap < (1ll << 30), "key count must be in [0, 2^30) (got %lld)",
-              (long long)cap);
-  GSX_REQUIRE(nth > 0 && ntw > 0, "tile grid must be positive (got %d x %d)", ntw, nth);
-  GSX_REQUIRE((int64_t)nth * ntw < (1ll << 31), "too many tiles");
-  return GSX_OK;
 }
 
 int gsx_tile_culling_aabb_start_end(int64_t n, int64_t n_keys,

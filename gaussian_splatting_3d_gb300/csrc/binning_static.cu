@@ -27,29 +27,81 @@ constexpr size_t kStaticScratchBytes = size_t(64) << 20;
 
 static __device__ __align__(256) unsigned char g_binning_scratch[kStaticScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_scratch_mutex;
-void *g_scratch_addr[kMaxDevices] = {};
+// The array's device address belongs to one CUDA context: the runtime's
+// primary context of a device, or a context the caller created and made
+// current with the driver API, or the new primary context after a
+// cudaDeviceReset.  Addresses are therefore cached per context, keyed by the
+// context's unique id (cuCtxGetId: never reused within a process), not per
+// device ordinal.  The two driver functions are reached through the
+// runtime's entry-point query, so the library does not link libcuda.
+using CtxGetCurrentFn = int (*)(void **ctx);
+using CtxGetIdFn = int (*)(void *ctx, unsigned long long *id);
 
-// Device address of g_binning_scratch on the current device, looked up once
-// per device.  In host code the array's name is only a host-side stand-in,
-// so the address must come from cudaGetSymbolAddress with the device current.
+constexpr int kCacheSlots = 64;
+struct ScratchSlot {
+  unsigned long long ctx_id;
+  void *addr;
+};
+std::mutex g_scratch_mutex;
+ScratchSlot g_scratch_cache[kCacheSlots] = {};
+int g_scratch_next = 0;  // round-robin replacement once every slot is used
+bool g_driver_looked_up = false;
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+void look_up_driver_functions() {
+  if (g_driver_looked_up) return;
+  g_driver_looked_up = true;
+  cudaDriverEntryPointQueryResult q;
+  void *f = nullptr;
+  if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+          cudaSuccess &&
+      q == cudaDriverEntryPointSuccess)
+    g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+  f = nullptr;
+  if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+          cudaSuccess &&
+      q == cudaDriverEntryPointSuccess)
+    g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f);
+  cudaGetLastError();  // a failed query leaves no sticky runtime error behind
+}
+
+// Id of the context current on this thread; false if there is none (or the
+// driver functions are unavailable).
+bool current_context_id(unsigned long long *id) {
+  if (!g_ctx_get_current || !g_ctx_get_id) return false;
+  void *ctx = nullptr;
+  if (g_ctx_get_current(&ctx) != 0 || ctx == nullptr) return false;
+  return g_ctx_get_id(ctx, id) == 0;
+}
+
+// Device address of g_binning_scratch in the current context.  In host code
+// the array's name is only a host-side stand-in, so the address must come
+// from cudaGetSymbolAddress with the device (and context) current.  It is
+// looked up once per context and cached; if the context cannot be
+// identified, it is looked up on every call.
 int scratch_address(void **out) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
-  if (dev < 0 || dev >= kMaxDevices) {
-    set_error("device ordinal %d is outside the supported range [0, %d)", dev, kMaxDevices);
-    return GSX_ERR_INVALID_ARG;
-  }
   std::lock_guard<std::mutex> lock(g_scratch_mutex);
-  if (g_scratch_addr[dev] == nullptr) {
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_binning_scratch);
-    if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(binning scratch)");
-    g_scratch_addr[dev] = p;
+  look_up_driver_functions();
+  unsigned long long id = 0;
+  bool have_id = current_context_id(&id);
+  if (have_id) {
+    for (const ScratchSlot &s : g_scratch_cache)
+      if (s.addr != nullptr && s.ctx_id == id) {
+        *out = s.addr;
+        return GSX_OK;
+      }
   }
-  *out = g_scratch_addr[dev];
+  void *p = nullptr;
+  // also makes the device's primary context current if no context was
+  cudaError_t e = cudaGetSymbolAddress(&p, g_binning_scratch);
+  if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(binning scratch)");
+  if (!have_id) have_id = current_context_id(&id);
+  if (have_id) {
+    g_scratch_cache[g_scratch_next] = ScratchSlot{id, p};
+    g_scratch_next = (g_scratch_next + 1) % kCacheSlots;
+  }
+  *out = p;
   return GSX_OK;
 }
 
@@ -62,16 +114,9 @@ extern "C" int gsx_tile_culling_aabb_start_end_noalloc(
     int64_t n, int64_t n_keys, const int32_t *aabb_topleft, const int32_t *aabb_bottomright,
     const float *depth, int32_t n_tiles_h, int32_t n_tiles_w, int32_t *gaussian_ids,
     int32_t *start, int32_t *end, void *stream) {
-  if (n < 0 || n >= (int64_t(1) << 30) || n_keys < 0 || n_keys >= (int64_t(1) << 30)) {
-    set_error("n and n_keys must be in [0, 2^30) (got %lld, %lld)", (long long)n,
-              (long long)n_keys);
-    return GSX_ERR_INVALID_ARG;
-  }
-  if (n_tiles_h <= 0 || n_tiles_w <= 0 || (int64_t)n_tiles_h * n_tiles_w >= (int64_t(1) << 31)) {
-    set_error("tile grid must be positive and below 2^31 tiles (got %d x %d)", n_tiles_w,
-              n_tiles_h);
-    return GSX_ERR_INVALID_ARG;
-  }
+  clear_error();
+  int st = check_binning_sizes(n, n_keys, n_tiles_h, n_tiles_w);
+  if (st != GSX_OK) return st;
   if (!start || !end || (n > 0 && (!aabb_topleft || !aabb_bottomright || !depth)) ||
       (n_keys > 0 && !gaussian_ids)) {
     set_error("null pointer argument");
@@ -87,7 +132,7 @@ extern "C" int gsx_tile_culling_aabb_start_end_noalloc(
     return GSX_ERR_CAPACITY;
   }
   void *scratch = nullptr;
-  int st = scratch_address(&scratch);
+  st = scratch_address(&scratch);
   if (st != GSX_OK) return st;
   int64_t got = 0;
   st = run_binning(n, aabb_topleft, aabb_bottomright, 2, nullptr, depth, n_tiles_w, n_tiles_h,

@@ -64,7 +64,11 @@ __device__ __forceinline__ bool sphere_in_frustum(float mx, float my, float mz,
 
 // Host-side helpers (implemented in abi.cu).
 void set_error(const char *fmt, ...);
+void clear_error();  // empties this thread's gsx_last_error message
 int cuda_status(cudaError_t e, const char *what);
+// Ranges every binning entry point accepts: n and the key count in [0, 2^30),
+// a positive tile grid of fewer than 2^31 tiles.
+int check_binning_sizes(int64_t n, int64_t cap, int32_t nth, int32_t ntw);
 // Counts kernel launches issued by this library (read by gsx_kernel_launch_count).
 void count_launches(unsigned n);
 

@@ -94,10 +94,14 @@ int gsx_tile_culling_aabb_start_end(int64_t n, int64_t n_keys,
  * (cudaMalloc can synchronise the device).  It takes no workspace and
  * allocates nothing; its scratch is a 64 MiB array in the library's static
  * device memory, which every GPU that loads the library holds until the
- * process exits.  Inputs whose scratch need exceeds 64 MiB (roughly
- * 16 bytes per Gaussian plus 16 bytes per key) are rejected with
- * GSX_ERR_CAPACITY.  The first call on each device looks up the array's
- * device address; make that first call before any stream capture.  All calls
+ * process exits.  Inputs are accepted when
+ * gsx_binning_workspace_bytes(n, n_keys, n_tiles_h * n_tiles_w) <= 64 MiB
+ * (about 17.0 bytes per Gaussian plus 17.4 bytes per key: some 1.9 million
+ * Gaussians with as many keys) and rejected with GSX_ERR_CAPACITY otherwise.
+ * The first call in each CUDA context (the device's primary context, or a
+ * context the caller made current) looks up the array's device address in
+ * that context; make that first call before any stream capture.  Like
+ * gsx_tile_culling_aabb_start_end it synchronises `stream` once.  All calls
  * share the array, so calls that overlap on the GPU (other streams, other
  * host threads) race and must be serialised by the caller.  This entry point
  * has no counterpart in the reference.

@@ -8,11 +8,12 @@ recipe therefore copies, at build time and only into the git-ignored
 (each prefixed by a #line directive naming the original file and line), and
 compiles them with ``oracle/ref_emu/ref_driver.cpp`` against the shim headers
 in ``oracle/ref_emu/shim``.  The reference's common.h, data_spec.h, kernels.h,
-shencoder.h and helper_math.h are included unmodified from
-/root/reference/gs/src/include.  Nothing from the reference is committed.
+shencoder.h and helper_math.h are included unmodified from the reference's
+gs/src/include.  Nothing from the reference is committed.
 
-Only this container has /root/reference; elsewhere ``reference_available()``
-is False and nothing is built.
+The reference checkout is taken from $GSX_REFERENCE_DIR (default
+/root/reference, where the build container mounts it); where it is absent
+``reference_available()`` is False and nothing is built.
 """
 from __future__ import annotations
 
@@ -21,7 +22,9 @@ import os
 import subprocess
 from pathlib import Path
 
-REF = Path("/root/reference")
+# the reference checkout: $GSX_REFERENCE_DIR, else where this build's
+# container mounts it
+REF = Path(os.environ.get("GSX_REFERENCE_DIR", "/root/reference"))
 INC = REF / "gs" / "src" / "include"
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"

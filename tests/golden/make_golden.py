@@ -26,6 +26,7 @@ them; tests/test_gpu_golden.py checks the CUDA path.
 from __future__ import annotations
 
 import ctypes
+import os
 import sys
 import types
 from pathlib import Path
@@ -35,7 +36,9 @@ import torch
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
-REF = Path("/root/reference")
+# the reference checkout: $GSX_REFERENCE_DIR, else where this build's
+# container mounts it
+REF = Path(os.environ.get("GSX_REFERENCE_DIR", "/root/reference"))
 sys.path.insert(0, str(ROOT))
 
 from oracle import build_ref  # noqa: E402

@@ -76,3 +76,25 @@ def test_shrenderer_save_load(tmp_path):
     q = SHRenderer.load(tmp_path / "s.pt", device="cpu")
     for k in ck.PARAM_KEYS:
         assert torch.equal(getattr(q, k).data, getattr(r, k).data)
+
+
+class _RunsCode:
+    """Pickles as a call of an importable function (here ``os.getpid`` on
+    load): a checkpoint must not be able to make the loader call it."""
+
+    def __reduce__(self):
+        import os
+
+        return (os.getpid, ())
+
+
+def test_checkpoint_cannot_call_importable_functions(tmp_path):
+    p = params()
+    torch.save({"mean": p[0], "qvec": p[1], "svec_before_activation": p[2], "sh_coeffs": p[3],
+                "alpha_before_activation": p[4], "N": 7, "cfg": _RunsCode()}, tmp_path / "evil.pt",
+               pickle_module=pickle)
+    sd = ck.load_state(tmp_path / "evil.pt")
+    # the named function was replaced by an inert stand-in, not called
+    assert isinstance(sd["cfg"], ck.Opaque)
+    assert type(sd["cfg"]).__module__.startswith("gsx_missing.")
+    assert torch.equal(sd["mean"], p[0])

@@ -8,7 +8,8 @@ in the library's static device memory instead of taking a workspace.  This
 test calls both entry points through the C ABI on the same inputs, twice in a
 row with different scenes (so leftovers of the first call in the shared
 array would show), and requires identical gaussian_ids / start / end -- the
-exact-match tolerance every binning test uses.  It lives in its own file that
+exact-match tolerance every binning test uses -- and the same lists from the
+CPU oracle's restatement of the reference binning.  It lives in its own file that
 pytest collects last, and passes both alone and after the other tests.
 """
 import ctypes
@@ -61,6 +62,7 @@ def _bin(entry, tl, br, depth, K, ntw, nth, with_workspace):
         st = getattr(lib, entry)(n, K, t_tl.data_ptr(), t_br.data_ptr(), t_depth.data_ptr(), nth, ntw,
                                  ids.data_ptr(), start.data_ptr(), end.data_ptr(), stream)
     _lib.check(st, entry)
+    assert lib.gsx_last_error() == b""  # a successful call leaves no earlier message behind
     torch.cuda.synchronize()
     return ids.cpu().numpy(), start.cpu().numpy(), end.cpu().numpy()
 
@@ -72,6 +74,11 @@ def test_noalloc_binning_matches_workspace_binning_on_consecutive_calls():
         got = _bin("gsx_tile_culling_aabb_start_end_noalloc", tl, br, depth, K, ntw, nth, False)
         for a, b in zip(got, ref):
             np.testing.assert_array_equal(a, b)
+        orc = O.bin_gaussians(tl, br, depth, nth, ntw)
+        assert orc["K"] == K
+        np.testing.assert_array_equal(got[0], orc["ids"][:K])
+        np.testing.assert_array_equal(got[1], orc["start"])
+        np.testing.assert_array_equal(got[2], orc["end"])
 
 
 def test_noalloc_rejects_inputs_beyond_its_scratch():
