@@ -14,10 +14,11 @@ device->host copy of the image, the loss and all gradients inside the timed
 region (the SH upload overlaps projection and binning, the image download
 overlaps the backward); ``roofline`` for the dominant kernel from
 per-stage CUDA events inside the timed region; ``cpu_baseline`` = the CPU
-oracle on a bounded sample of the same workload.
+oracle on whole steps of the same workload (median of a few).
 
 ``--impl reference`` times the reference's path on the host CPU cores (the C
-restatement of its kernels in oracle/, all threads) on the same workload.
+restatement of its kernels in oracle/, all threads) on the same workload,
+every step whole, and prints the same ``config``.
 With --gpus N > 1 every rank renders its own replica (views are independent);
 there is no collective.
 """
@@ -309,13 +310,7 @@ def run_gsx(args):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded PCG64 scene of the headline shape; no dataset)",
-        "config": {"workload": f"{args.workload}: {sc.n} Gaussians, SH degree {sc.sh_order - 1}, "
-                               f"{view.cam.w}x{view.cam.h}, tile {view.tile}x{view.tile}, fwd+bwd",
-                   "n_gaussians": sc.n, "visible": visible, "keys": K, "width": view.cam.w,
-                   "height": view.cam.h, "sh_degree": sc.sh_order - 1, "tile": view.tile,
-                   "l2": "inputs larger than L2 (scene parameters %.0f MB)" % (
-                       sum(p.numel() * 4 for p in params) / 1e6),
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": workload_config(wl, args.workload, visible, K, world),
         "stages_ms": {k: round(v["mean_ms"], 4) for k, v in stages.items()},
         "e2e": {"value": round(e2e_ms, 4), "unit": "ms/iter", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
@@ -353,14 +348,28 @@ def run_gsx(args):
         line["metric"] += ", per-Gaussian SH colours"
         line["config"]["sh_mode"] = "gaussian: one SH colour per Gaussian per view (opt-in, not the reference's images)"
     elif not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(wl, args.cpu_frac)
+        line["cpu_baseline"] = cpu_baseline(wl, args.cpu_iters)
     print(json.dumps(line), flush=True)
 
 
-def cpu_baseline(wl, frac: float):
-    """The CPU oracle (C restatement of the reference's kernels, OpenMP over
-    tiles) on a bounded sample: projection and binning on the whole scene,
-    raster forward + backward on every k-th tile row, scaled to the frame."""
+def workload_config(wl, workload: str, visible: int, keys: int, world: int) -> dict:
+    """The ``config`` of the headline-style lines, shared by the GPU arm and
+    the reference arm so both name the same workload."""
+    sc, view = wl.scene, wl.views[0]
+    param_mb = (sc.mean.nbytes + sc.qvec.nbytes + sc.log_scale.nbytes + sc.sh.nbytes + sc.alpha_logit.nbytes) / 1e6
+    return {"workload": f"{workload}: {sc.n} Gaussians, SH degree {sc.sh_order - 1}, "
+                        f"{view.cam.w}x{view.cam.h}, tile {view.tile}x{view.tile}, fwd+bwd",
+            "n_gaussians": sc.n, "visible": int(visible), "keys": int(keys), "width": view.cam.w,
+            "height": view.cam.h, "sh_degree": sc.sh_order - 1, "tile": view.tile,
+            "l2": "inputs larger than L2 (scene parameters %.0f MB)" % param_mb,
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
+def oracle_step(wl):
+    """One whole step of the workload on the CPU oracle (the C restatement of
+    the reference's kernels, OpenMP over tiles): projection with culling,
+    binning, raster forward and backward over every tile of the frame,
+    projection backward.  Returns (seconds, visible Gaussians, keys)."""
     from oracle import oracle as O
     from gaussian_splatting_3d_gb300.camera import frustum_np
 
@@ -372,61 +381,79 @@ def cpu_baseline(wl, frac: float):
     pr = O.project(sc.mean, sc.qvec, sc.log_scale, sc.alpha_logit, ocam, 1.0, 6.0, view.tile, view.tile)
     ntw, nth = (cam.w + view.tile - 1) // view.tile, (cam.h + view.tile - 1) // view.tile
     b = O.bin_gaussians(pr["rect"], pr["rect"][:, 2:], pr["depth"], nth, ntw, stride=4)
-    t1 = time.perf_counter()
-    every = max(1, int(round(1.0 / frac)))
-    rows = np.arange(nth) % every == 0
-    start = b["start"].reshape(nth, ntw).copy()
-    end = b["end"].reshape(nth, ntw).copy()
-    start[~rows] = -1
-    end[~rows] = -1
     P = O.raster_params(cam.w, cam.h, view.tile, view.tile, sc.sh_order, sc.sh.shape[-1])
     tl = np.array(cam.topleft(), np.float32)
     psx, psy = np.float32(1 / cam.fx), np.float32(1 / cam.fy)
-    t2 = time.perf_counter()
-    img = O.render_fwd(P, pr["mean2d"], pr["cov2d"], sc.sh, pr["alpha"], start.reshape(-1), end.reshape(-1),
-                       b["ids"], tl, view.c2w, psx, psy)
-    g = O.render_bwd(P, pr["mean2d"], pr["cov2d"], sc.sh, pr["alpha"], start.reshape(-1), end.reshape(-1),
-                     b["ids"], tl, view.c2w, psx, psy, img, wl.grad_weight)
+    img = O.render_fwd(P, pr["mean2d"], pr["cov2d"], sc.sh, pr["alpha"], b["start"], b["end"], b["ids"], tl,
+                       view.c2w, psx, psy)
+    g = O.render_bwd(P, pr["mean2d"], pr["cov2d"], sc.sh, pr["alpha"], b["start"], b["end"], b["ids"], tl,
+                     view.c2w, psx, psy, img, wl.grad_weight)
     O.project_bwd(sc.mean, sc.qvec, sc.log_scale, sc.alpha_logit, ocam, pr["mask"], g["mean2d"], g["cov2d"],
                   g["alpha"])
-    t3 = time.perf_counter()
-    sampled = float(rows.sum()) / nth
-    total_s = (t1 - t0) + (t3 - t2) / sampled
-    return {"value": round(total_s * 1e3, 1), "unit": "ms/iter", "cores": O.num_threads(), "kind": "port",
-            "sample": f"projection + binning on all {sc.n} Gaussians; raster fwd+bwd on every {every}-th tile row "
-                      f"({int(rows.sum())}/{nth} rows), time scaled by {1 / sampled:.2f}"}
+    return time.perf_counter() - t0, int(pr["mask"].sum()), int(b["K"])
+
+
+def cpu_stats(times_s) -> dict:
+    ms = np.asarray(times_s, np.float64) * 1e3
+    return {"median": round(float(np.median(ms)), 1), "p99": round(float(np.percentile(ms, 99)), 1),
+            "mean": round(float(ms.mean()), 1), "min": round(float(ms.min()), 1), "n": int(ms.size)}
+
+
+def cpu_baseline(wl, iters: int) -> dict:
+    """The CPU oracle on whole frames of the workload: one warm-up step, then
+    `iters` timed steps (each one full forward + backward, nothing scaled);
+    value = the median step time."""
+    from oracle import oracle as O
+
+    oracle_step(wl)
+    times = [oracle_step(wl)[0] for _ in range(max(1, iters))]
+    st = cpu_stats(times)
+    return {"value": st["median"], "unit": "ms/iter", "cores": O.num_threads(), "kind": "port",
+            "stats_ms": st,
+            "sample": f"{st['n']} whole steps after 1 warm-up (projection, binning, raster fwd+bwd on all tiles, "
+                      f"projection bwd); value = median"}
 
 
 def run_reference(args):
+    """The reference's path on the host CPU cores: the C restatement of its
+    kernels (the reference has no CPU implementation of them, and its
+    sources do not travel to the GPU host), every tile of every step, all
+    host threads.  --warmup untimed steps, then --steps timed steps; value =
+    the median step time, the sum of the step times is the timed region."""
     rank, world, local = dist_env()
     if rank != 0:
         return
     from gaussian_splatting_3d_gb300 import scene as S
+    from oracle import oracle as O
 
     wl = S.headline_workload(n=args.n) if args.workload == "headline" else S.small_workload()
     for _ in range(args.warmup):
-        cpu_baseline(wl, args.cpu_frac)
-    vals = [cpu_baseline(wl, args.cpu_frac) for _ in range(args.steps)]
-    v = float(np.mean([x["value"] for x in vals]))
-    sc, view = wl.scene, wl.views[0]
+        oracle_step(wl)
+    runs = [oracle_step(wl) for _ in range(args.steps)]
+    times = [r[0] for r in runs]
+    st = cpu_stats(times)
+    v = st["median"]
     line = {
         "impl": "reference",
         "metric": "fwd+bwd ms/iter (1M Gaussians, 1920x1080)",
-        "value": round(v, 1),
+        "value": v,
         "unit": "ms/iter",
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": round(v, 1),
+        "ms_per_step": v,
         "higher_is_better": False,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded PCG64 scene of the headline shape; no dataset)",
-        "config": {"workload": f"{args.workload}: {sc.n} Gaussians, SH degree {sc.sh_order - 1}, "
-                               f"{view.cam.w}x{view.cam.h}, tile {view.tile}x{view.tile}, fwd+bwd"},
-        "cpu_baseline": dict(vals[-1], value=round(v, 1)),
-        "e2e": {"value": round(v, 1), "unit": "ms/iter", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "config": workload_config(wl, args.workload, runs[-1][1], runs[-1][2], world),
+        "cpu_baseline": {"value": v, "unit": "ms/iter", "cores": O.num_threads(), "kind": "port",
+                         "stats_ms": st,
+                         "sample": f"every step whole: projection, binning, raster fwd+bwd on all tiles, projection "
+                                   f"bwd; {args.steps} timed steps after {args.warmup} warm-up; value = median"},
+        "timed_region_s": round(float(np.sum(times)), 3),
+        "e2e": {"value": v, "unit": "ms/iter", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
@@ -674,7 +701,8 @@ def run_reference_cuda(args):
     not run again."""
     print(json.dumps({"impl": "reference-cuda", "unavailable":
                       "the reference's CUDA backward trips its own device assert (vol_render_sh.h:448-452: "
-                      "recomputed colour != stored colour) on GB300; faulting reference GPU code is not re-run"}))
+                      "recomputed colour != stored colour) on GB300 (Xid 43; the call's log was not kept); "
+                      "faulting reference GPU code is not re-run"}))
 
 def run_train(args):
     """One training iteration of the reference's loop (main_sh.py:150-240) on
@@ -769,7 +797,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sh-mode", default="pixel", choices=["pixel", "gaussian"],
                     help="headline: SH colour per pixel (the reference) or per Gaussian (opt-in)")
-    ap.add_argument("--cpu-frac", type=float, default=1.0 / 8.0)
+    ap.add_argument("--cpu-iters", type=int, default=5, help="whole CPU-oracle steps timed for cpu_baseline")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -12,6 +12,7 @@ import json
 import os
 import subprocess
 import sys
+import time
 
 import pytest
 
@@ -21,9 +22,12 @@ sys.path.insert(0, ROOT)
 import bench  # noqa: E402
 
 
-def _run(*args, timeout=600):
+def _run(*args, timeout=600, wall=None):
+    t0 = time.perf_counter()
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), *args], cwd=ROOT,
                        capture_output=True, text=True, timeout=timeout)
+    if wall is not None:
+        wall.append(time.perf_counter() - t0)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
     assert len(lines) == 1, r.stdout
@@ -32,7 +36,8 @@ def _run(*args, timeout=600):
 
 def test_reference_arm_line_on_the_small_workload():
     pytest.importorskip("torch")
-    d = _run("--impl", "reference", "--workload", "small", "--steps", "1", "--warmup", "3")
+    wall = []
+    d = _run("--impl", "reference", "--workload", "small", "--steps", "3", "--warmup", "3", wall=wall)
     for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
               "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
         assert k in d, k
@@ -42,6 +47,15 @@ def test_reference_arm_line_on_the_small_workload():
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": "ms/iter", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["config"]["workload"].startswith("small")
+    # a measurement of whole steps, not an extrapolation: the claimed step
+    # time over the timed steps fits inside the process's own wall time
+    assert d["value"] * 1e-3 * d["steps"] <= wall[0]
+    assert cb["stats_ms"]["n"] == 3 and cb["stats_ms"]["p99"] >= cb["stats_ms"]["median"]
+    # the same config keys the GPU arm prints (visible Gaussians and keys from the oracle)
+    from gaussian_splatting_3d_gb300 import scene as S
+
+    want = bench.workload_config(S.small_workload(), "small", d["config"]["visible"], d["config"]["keys"], 1)
+    assert d["config"] == want and d["config"]["keys"] > 0
 
 
 def test_reference_cuda_arm_is_unavailable():
