@@ -103,15 +103,24 @@ class ClockSampler:
         self.proc = None
         self.path = None
 
-    def start(self):
+    def start(self, wait_s: float = 3.0):
+        """Start sampling and return once the first sample is written (or
+        after `wait_s`): nvidia-smi's start-up queries the driver, so it
+        must not overlap a timed region."""
         fd, self.path = tempfile.mkstemp(suffix=".csv")
         os.close(fd)
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < wait_s and self.proc.poll() is None:
+            if os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.02)
 
     def stop(self):
         if self.proc is None:
@@ -193,7 +202,8 @@ def run_gsx(args):
         dist.init_process_group("nccl", device_id=dev)
     wl = S.headline_workload(n=args.n) if args.workload == "headline" else S.small_workload()
     sc, view = wl.scene, wl.views[0]
-    settings = renderer.RasterSettings(tile_w=view.tile, tile_h=view.tile, sh_mode=args.sh_mode)
+    settings = renderer.RasterSettings(tile_w=view.tile, tile_h=view.tile, sh_mode=args.sh_mode,
+                                       pixels_per_thread=args.pixels_per_thread)
     params = [torch.from_numpy(a).to(dev) for a in (sc.mean, sc.qvec, sc.log_scale, sc.sh, sc.alpha_logit)]
     W = torch.from_numpy(wl.grad_weight).to(dev)
     pipe = renderer.ViewPipeline(dev)
@@ -203,6 +213,9 @@ def run_gsx(args):
         grads = pipe.backward(state, *params, W, timer=timer)
         return state, grads
 
+    # the clock sampler runs from before the warm-up through the timed region
+    clocks = ClockSampler(local)
+    clocks.start()
     for _ in range(args.warmup):
         state, grads = step()
     torch.cuda.synchronize()
@@ -218,11 +231,9 @@ def run_gsx(args):
 
     from gaussian_splatting_3d_gb300 import _lib
 
-    clocks = ClockSampler(local)
     timer = renderer.StageTimer()
     barrier()
     launches0 = _lib.load().gsx_kernel_launch_count()
-    clocks.start()
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     wall0 = time.perf_counter()
@@ -797,6 +808,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sh-mode", default="pixel", choices=["pixel", "gaussian"],
                     help="headline: SH colour per pixel (the reference) or per Gaussian (opt-in)")
+    ap.add_argument("--pixels-per-thread", type=int, default=0, choices=[0, 1, 2],
+                    help="raster backward schedule (0: two pixels per thread where the tile allows)")
     ap.add_argument("--cpu-iters", type=int, default=5, help="whole CPU-oracle steps timed for cpu_baseline")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -11,7 +11,7 @@ from ctypes import POINTER, c_char_p, c_float, c_int, c_int32, c_int64, c_size_t
 
 from . import _build
 
-GSX_ABI_VERSION = 2  # include/gsx.h
+GSX_ABI_VERSION = 3  # include/gsx.h
 GSX_OK = 0
 GSX_ERR_INVALID_ARG = 1
 GSX_ERR_CAPACITY = 2
@@ -64,6 +64,7 @@ class GsxRasterParams(ctypes.Structure):
         ("pixel_size_y", c_float),
         ("T_thresh", c_float),
         ("write_empty_tiles", c_int32),
+        ("pixels_per_thread", c_int32),
     ]
 
 

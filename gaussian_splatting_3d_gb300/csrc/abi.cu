@@ -202,6 +202,8 @@ static int check_raster(const RasterArgs &a, int C, int64_t n, int64_t n_keys) {
               "tile grid %d x %d of %d x %d tiles does not cover %d x %d", a.n_tiles_w,
               a.n_tiles_h, a.tile_w, a.tile_h, a.width, a.height);
   GSX_REQUIRE(a.sh_stride >= C * C, "sh_stride %d < C*C", a.sh_stride);
+  GSX_REQUIRE(a.pixels_per_thread >= 0 && a.pixels_per_thread <= 2,
+              "pixels_per_thread must be 0, 1 or 2 (got %d)", a.pixels_per_thread);
   GSX_REQUIRE(n >= 0 && n_keys >= 0, "negative size");
   GSX_REQUIRE(a.start && a.end && a.topleft && a.c2w && a.out, "null pointer argument");
   GSX_REQUIRE(n_keys == 0 || a.ids, "null gaussian_ids");
@@ -327,6 +329,7 @@ static int render_forward(const gsx_raster_params *p, int64_t n, int64_t n_keys,
   RasterArgs a = make_args(p->tile_w, p->tile_h, (uint32_t)p->n_tiles_w,
                            (uint32_t)p->n_tiles_h, p->pixel_size_x, p->pixel_size_y,
                            (uint32_t)p->height, (uint32_t)p->width, p->T_thresh);
+  a.pixels_per_thread = p->pixels_per_thread;
   a.sh_stride = p->sh_stride;
   a.mean2d = mean2d;
   a.cov2d = cov2d;
@@ -392,6 +395,7 @@ int gsx_render_forward_rgb(const gsx_raster_params *p, int64_t n, int64_t n_keys
   RasterArgs a = make_args(p->tile_w, p->tile_h, (uint32_t)p->n_tiles_w,
                            (uint32_t)p->n_tiles_h, p->pixel_size_x, p->pixel_size_y,
                            (uint32_t)p->height, (uint32_t)p->width, p->T_thresh);
+  a.pixels_per_thread = p->pixels_per_thread;
   a.sh_stride = 1;  // rgb [n,3] as one coefficient per channel
   a.mean2d = mean2d;
   a.cov2d = cov2d;
@@ -424,6 +428,7 @@ int gsx_render_backward_rgb(const gsx_raster_params *p, int64_t n, int64_t n_key
   RasterArgs a = make_args(p->tile_w, p->tile_h, (uint32_t)p->n_tiles_w,
                            (uint32_t)p->n_tiles_h, p->pixel_size_x, p->pixel_size_y,
                            (uint32_t)p->height, (uint32_t)p->width, p->T_thresh);
+  a.pixels_per_thread = p->pixels_per_thread;
   a.sh_stride = 1;
   a.mean2d = mean2d;
   a.cov2d = cov2d;
@@ -511,6 +516,7 @@ static int render_backward(const gsx_raster_params *p, int64_t n, int64_t n_keys
   RasterArgs a = make_args(p->tile_w, p->tile_h, (uint32_t)p->n_tiles_w,
                            (uint32_t)p->n_tiles_h, p->pixel_size_x, p->pixel_size_y,
                            (uint32_t)p->height, (uint32_t)p->width, p->T_thresh);
+  a.pixels_per_thread = p->pixels_per_thread;
   a.sh_stride = p->sh_stride;
   a.mean2d = mean2d;
   a.cov2d = cov2d;

@@ -42,6 +42,27 @@ __device__ __forceinline__ float gsx_expf(float x) {
   return p * __int_as_float((ji + 127) << 23);
 }
 
+// gsx_expf for x in [-86, 0], the range of every raster decision: the same
+// operation sequence without the range branches, and j taken from the bits
+// of the rounding sum t = 1.5 * 2^23 + j (exact for |j| < 2^22) instead of a
+// float -> int conversion, so it returns gsx_expf(x) bit for bit there.
+__device__ __forceinline__ float gsx_expf_neg(float x) {
+  float t = fmaf(x, 1.44269502162933349609375f, 12582912.0f);
+  float j = t - 12582912.0f;
+  float r = fmaf(j, -0.693145751953125f, x);
+  r = fmaf(j, -1.428606765330187045e-06f, r);
+  float p = 1.98412698412698412e-04f;
+  p = fmaf(p, r, 1.38888888888888889e-03f);
+  p = fmaf(p, r, 8.33333333333333333e-03f);
+  p = fmaf(p, r, 4.16666666666666667e-02f);
+  p = fmaf(p, r, 1.66666666666666667e-01f);
+  p = fmaf(p, r, 0.5f);
+  p = fmaf(p, r, 1.0f);
+  p = fmaf(p, r, 1.0f);
+  const int ji = __float_as_int(t) - 0x4B400000;  // t = 12582912 + j
+  return p * __int_as_float((ji + 127) << 23);
+}
+
 __device__ __forceinline__ float gsx_sigmoidf(float x) {
   return 1.0f / (1.0f + gsx_expf(-x));
 }
@@ -157,6 +178,9 @@ struct RasterArgs {
   // single view: CTA b renders tile tile_order[b] (a permutation of the tiles,
   // longest lists first); nullptr renders tile b
   const int32_t *tile_order;
+  // raster backward: 1 = one pixel per thread, 2 = two (tiles made of 8x8
+  // blocks only), 0 = two wherever possible
+  int32_t pixels_per_thread;
 };
 int launch_raster_forward(const RasterArgs &a, int C, cudaStream_t s);
 // order[0..n_tiles) = the tiles by descending list length (end - start), in

@@ -38,6 +38,8 @@
 // high and low parts, three products, FP32 accumulation: ~2^-21 relative per
 // product).  Warp results meet in shared memory (atomics), and the CTA issues
 // one global atomic per (tile, Gaussian, value).
+#include <cuda_fp16.h>
+
 #include "gsx_internal.cuh"
 
 namespace gsx {
@@ -817,13 +819,68 @@ __device__ __forceinline__ void flush_sh_group(const float *Ws, const float *Ys,
     }
 }
 
+// Adds the batch's per-Gaussian accumulators (s_grad, kept Gaussians whose
+// s_touched is set) into the global gradients: one vector reduction per chunk
+// of a record -- mean2d (v2), cov2d (v4, entries 1 and 2 both get dL/dcov01 as
+// the reference writes them), alpha, and the SH channels in 4-float chunks.
+template <int C>
+__device__ __forceinline__ void fold_batch_grads(const RasterArgs &a, const ViewCtx &ctx,
+                                                 const SmemLayout &L, const float *s_grad,
+                                                 const int *s_touched, int nk, int t, int nthr) {
+  constexpr int CC = Sh<C>::CC, NV = Grad<C>::NV;
+  constexpr int NCH = Grad<C>::CSTR / 4;
+  constexpr int NCHUNK = 3 + 3 * NCH;
+  for (int f = t; f < nk * NCHUNK; f += nthr) {
+    const int j = f / NCHUNK, c = f - j * NCHUNK;
+    if (!s_touched[j]) continue;
+    const float *rec = s_grad + j * NV;
+    const int64_t id = L.ids[j];
+    if (c == 0) {
+      const float2 v = *reinterpret_cast<const float2 *>(rec);
+      if (a.vec_grads) {
+        if (v.x != 0.0f || v.y != 0.0f) red_add_v2(a.g_mean2d + 2 * id, v);
+      } else {
+        if (v.x != 0.0f) atomicAdd(a.g_mean2d + 2 * id, v.x);
+        if (v.y != 0.0f) atomicAdd(a.g_mean2d + 2 * id + 1, v.y);
+      }
+    } else if (c == 1) {
+      const float4 v = make_float4(rec[2], rec[3], rec[3], rec[4]);
+      if (a.vec_grads) {
+        if (v.x != 0.0f || v.y != 0.0f || v.w != 0.0f) red_add_v4(a.g_cov2d + 4 * id, v);
+      } else {
+        if (v.x != 0.0f) atomicAdd(a.g_cov2d + 4 * id, v.x);
+        if (v.y != 0.0f) {
+          atomicAdd(a.g_cov2d + 4 * id + 1, v.y);
+          atomicAdd(a.g_cov2d + 4 * id + 2, v.y);
+        }
+        if (v.w != 0.0f) atomicAdd(a.g_cov2d + 4 * id + 3, v.w);
+      }
+    } else if (c == 2) {
+      if (rec[5] != 0.0f) atomicAdd(a.g_alpha + id, rec[5]);
+    } else {
+      const int e = c - 3, ch = e / NCH, k = 4 * (e - ch * NCH);
+      const float4 v = *reinterpret_cast<const float4 *>(rec + kShOff + ch * Grad<C>::CSTR + k);
+      if (v.x == 0.0f && v.y == 0.0f && v.z == 0.0f && v.w == 0.0f) continue;
+      float *dst = ctx.g_sh + ((id - ctx.item_lo) * 3 + ch) * ctx.sh_stride + k;
+      if (k + 4 <= CC && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+        red_add_v4(dst, v);
+      } else {
+        const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (k + q < CC && vv[q] != 0.0f) atomicAdd(dst + q, vv[q]);
+      }
+    }
+  }
+}
+
 // RGB: as in the forward; the gradient staged for the C = 1 reduction is
 // then dL/drgb itself (the constant basis makes the product a plain sum).
 template <int C, int MAXT, bool BATCHED, bool RGB = false>
 __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1)
     raster_backward_kernel(const RasterArgs a) {
   constexpr int CC = Sh<C>::CC, CCP = Sh<C>::CCP, GSH = Sh<C>::GSH;
-  constexpr int NV = Grad<C>::NV, CSTR = Grad<C>::CSTR;  // gm0 gm1 gc0 gc12 gc3 galpha gsh
+  constexpr int NV = Grad<C>::NV;  // gm0 gm1 gc0 gc12 gc3 galpha gsh
   extern __shared__ float4 smem4[];
   __shared__ int s_wcount[32];
   __shared__ uint64_t s_bar;  // bulk-copy barrier of the SH rows
@@ -975,53 +1032,371 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
     }
     if (!done && T < thr) done = true;
     __syncthreads();
-    // one vector reduction per chunk of a touched Gaussian's record: mean2d
-    // (v2), cov2d (v4, entries 1 and 2 both get dL/dcov01 as the reference
-    // writes them), alpha, and the SH channels in 4-float chunks
-    constexpr int NCH = Grad<C>::CSTR / 4;
-    constexpr int NCHUNK = 3 + 3 * NCH;
-    for (int f = t; f < nk * NCHUNK; f += nthr) {
-      const int j = f / NCHUNK, c = f - j * NCHUNK;
-      if (!s_touched[j]) continue;
-      const float *rec = s_grad + j * NV;
-      const int64_t id = L.ids[j];
-      if (c == 0) {
-        const float2 v = *reinterpret_cast<const float2 *>(rec);
-        if (a.vec_grads) {
-          if (v.x != 0.0f || v.y != 0.0f) red_add_v2(a.g_mean2d + 2 * id, v);
-        } else {
-          if (v.x != 0.0f) atomicAdd(a.g_mean2d + 2 * id, v.x);
-          if (v.y != 0.0f) atomicAdd(a.g_mean2d + 2 * id + 1, v.y);
-        }
-      } else if (c == 1) {
-        const float4 v = make_float4(rec[2], rec[3], rec[3], rec[4]);
-        if (a.vec_grads) {
-          if (v.x != 0.0f || v.y != 0.0f || v.w != 0.0f) red_add_v4(a.g_cov2d + 4 * id, v);
-        } else {
-          if (v.x != 0.0f) atomicAdd(a.g_cov2d + 4 * id, v.x);
-          if (v.y != 0.0f) {
-            atomicAdd(a.g_cov2d + 4 * id + 1, v.y);
-            atomicAdd(a.g_cov2d + 4 * id + 2, v.y);
-          }
-          if (v.w != 0.0f) atomicAdd(a.g_cov2d + 4 * id + 3, v.w);
-        }
-      } else if (c == 2) {
-        if (rec[5] != 0.0f) atomicAdd(a.g_alpha + id, rec[5]);
-      } else {
-        const int e = c - 3, ch = e / NCH, k = 4 * (e - ch * NCH);
-        const float4 v = *reinterpret_cast<const float4 *>(rec + kShOff + ch * Grad<C>::CSTR + k);
-        if (v.x == 0.0f && v.y == 0.0f && v.z == 0.0f && v.w == 0.0f) continue;
-        float *dst = ctx.g_sh + ((id - ctx.item_lo) * 3 + ch) * ctx.sh_stride + k;
-        if (k + 4 <= CC && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
-          red_add_v4(dst, v);
-        } else {
-          const float vv[4] = {v.x, v.y, v.z, v.w};
+    fold_batch_grads<C>(a, ctx, L, s_grad, s_touched, nk, t, nthr);
+  }
+}
+
+// ---- backward with two pixels per thread -----------------------------------
+// The same per-pair arithmetic as raster_backward_kernel, with each warp
+// covering an 8x8 block of pixels: lane l owns pixel A = (l & 7, l >> 3) and
+// pixel B = A + (0, 4) of its warp's block, so one (warp, Gaussian) entry of
+// the per-warp lists covers 64 pixels.  On the headline scene this cuts the
+// entries that reach the reductions from 3.2 M to 1.9 M while the pixel
+// evaluations grow by 5 %: the record loads, the SH row loads, the six-scalar
+// butterfly, the weight staging and the shared-memory folds are paid once for
+// both pixels.  The decision path (radial, exponential, 1/255, T) stays exact
+// and per pixel; the colour and gradient terms of the two pixels run as
+// paired float2 operations.
+//
+// SH gradients: sum_p w_ch(p) Y_k(p) over the warp's 64 pixels as one
+// m16n8k16 tensor-core product per group of five Gaussians, in FP16 with a
+// high/low split of both operands (hi*hi + hi*lo + lo*hi, FP32 accumulation:
+// about 2^-21 relative per product; a weight below 2^-24 is lost, far below
+// the gradient tolerance).  Both operands are staged as half2 pairs
+// (pixel A, pixel B) of one lane, so a 32-bit word holds the two adjacent
+// k values a fragment register wants; rows are 32 words with the column
+// XOR-swizzled by (row & 7) << 2, which makes the fragment reads and the
+// per-lane writes free of bank conflicts without padding.  The basis is split
+// once per warp; the weights once per Gaussian.
+constexpr int kP2Cols = 32;  // half2 columns per staged row: 64 pixels
+
+__device__ __forceinline__ int p2_idx(int row, int col) {
+  return row * kP2Cols + (col ^ ((row & 7) << 2));
+}
+
+__device__ __forceinline__ void split_half2(float a, float b, uint32_t &hi, uint32_t &lo) {
+  const __half2 h = __floats2half2_rn(a, b);
+  const __half2 l = __floats2half2_rn(a - __low2float(h), b - __high2float(h));
+  hi = *reinterpret_cast<const uint32_t *>(&h);
+  lo = *reinterpret_cast<const uint32_t *>(&l);
+}
+
+__device__ __forceinline__ void mma_f16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
+                                        uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Staging of one warp: weights W[16 rows][64 px] and basis Y[16 k][64 px],
+// each as high and low half2 words.
+struct P2Stage {
+  uint32_t *wh, *wl, *yh, *yl;
+};
+constexpr int kP2StageWords = 4 * 16 * kP2Cols;
+
+// SH gradients of the staged Gaussians, D[r][k] = sum_p W[r][p] Y[p][k] for
+// rows r = 3*slot + channel, added into the batch accumulators.
+template <int C>
+__device__ __forceinline__ void flush_sh_group2(const P2Stage &S, const int *slots, int nslot,
+                                                float *s_grad, int lane) {
+  constexpr int CC = Sh<C>::CC;
+  constexpr int NT = (CC + 7) / 8;
+  constexpr int NV = Grad<C>::NV, CSTR = Grad<C>::CSTR;
+  const int g = lane >> 2, tq = lane & 3;
+  // hi*hi and the two cross products in separate accumulators: four short
+  // dependency chains per flush instead of one of twelve tensor-core latencies
+  float d[NT][4], dc[NT][4];
 #pragma unroll
-          for (int q = 0; q < 4; ++q)
-            if (k + q < CC && vv[q] != 0.0f) atomicAdd(dst + q, vv[q]);
+  for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) d[nt][e] = dc[nt][e] = 0.0f;
+#pragma unroll
+  for (int ks = 0; ks < 4; ++ks) {
+    const int c0 = 8 * ks + tq, c1 = c0 + 4;
+    const uint32_t ah[4] = {S.wh[p2_idx(g, c0)], S.wh[p2_idx(g + 8, c0)], S.wh[p2_idx(g, c1)],
+                            S.wh[p2_idx(g + 8, c1)]};
+    const uint32_t al[4] = {S.wl[p2_idx(g, c0)], S.wl[p2_idx(g + 8, c0)], S.wl[p2_idx(g, c1)],
+                            S.wl[p2_idx(g + 8, c1)]};
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) {
+      const int n = 8 * nt + g;
+      const uint32_t bh0 = S.yh[p2_idx(n, c0)], bh1 = S.yh[p2_idx(n, c1)];
+      const uint32_t bl0 = S.yl[p2_idx(n, c0)], bl1 = S.yl[p2_idx(n, c1)];
+      mma_f16(d[nt], ah, bh0, bh1);
+      mma_f16(dc[nt], ah, bl0, bl1);
+      mma_f16(dc[nt], al, bh0, bh1);
+    }
+  }
+  // this lane's two rows: r = g and g + 8, i.e. (slot, channel) pairs
+  const int rows = 3 * nslot;
+  const int sl0 = g / 3, sl1 = (g + 8) / 3;
+  const int base0 = g < rows ? slots[sl0] * NV + kShOff + (g - 3 * sl0) * CSTR : -1;
+  const int base1 = g + 8 < rows ? slots[sl1] * NV + kShOff + (g + 8 - 3 * sl1) * CSTR : -1;
+#pragma unroll
+  for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int base = (e & 2) ? base1 : base0;
+      const int k = 8 * nt + 2 * tq + (e & 1);
+      const float v = d[nt][e] + dc[nt][e];
+      if (base >= 0 && k < CC && v != 0.0f) atomicAdd(&s_grad[base + k], v);
+    }
+}
+
+// Pixels of thread t: 8x8 warp blocks over the tile (tile_w and tile_h
+// multiples of 8); pixel B lies four rows below pixel A.
+__device__ __forceinline__ void pixel_of2(const ViewCtx &c, int t, int &gx, int &gy) {
+  const int w = t >> 5, l = t & 31, bpr = c.tile_w >> 3;
+  gx = (c.tile % c.n_tiles_w) * c.tile_w + (w % bpr) * 8 + (l & 7);
+  gy = (c.tile / c.n_tiles_w) * c.tile_h + (w / bpr) * 8 + (l >> 3);
+}
+
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
+// Bounds of the pixel centres of this warp's 8x8 block (both pixels of every
+// lane).
+__device__ __forceinline__ float4 warp_block2(float px, float py0, float py1) {
+  float x0 = px, x1 = px, y0 = fminf(py0, py1), y1 = fmaxf(py0, py1);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    x0 = fminf(x0, __shfl_xor_sync(kFull, x0, o));
+    x1 = fmaxf(x1, __shfl_xor_sync(kFull, x1, o));
+    y0 = fminf(y0, __shfl_xor_sync(kFull, y0, o));
+    y1 = fmaxf(y1, __shfl_xor_sync(kFull, y1, o));
+  }
+  return make_float4(x0, x1, y0, y1);
+}
+
+template <int C, int MAXT, bool BATCHED, bool RGB = false>
+__global__ void __launch_bounds__(MAXT, MAXT <= 128 ? 4 : 512 / MAXT)
+    raster_backward2_kernel(const RasterArgs a) {
+  constexpr int CC = Sh<C>::CC, CCP = Sh<C>::CCP, GSH = Sh<C>::GSH;
+  constexpr int NV = Grad<C>::NV;
+  extern __shared__ float4 smem4[];
+  __shared__ int s_wcount[32];
+  __shared__ uint64_t s_bar;  // bulk-copy barrier of the SH rows
+  float *smem = reinterpret_cast<float *>(smem4);
+  const int B = a.batch;
+  const int nthr = blockDim.x, nwarps = nthr >> 5;
+  SmemLayout L = carve<C>(smem, B);
+  float *s_grad = L.sh + B * GSH;                                              // [B][NV]
+  uint32_t *s_stage = reinterpret_cast<uint32_t *>(s_grad + B * NV);          // [nwarps][4][16][32]
+  int *s_slots = reinterpret_cast<int *>(s_stage + nwarps * kP2StageWords);  // [nwarps][8]
+  int *s_touched = s_slots + nwarps * 8;                                       // [B]
+  int *wl = s_touched + B + (threadIdx.x >> 5) * B;                            // [nwarps][B]
+
+  const ViewCtx ctx = make_ctx<BATCHED>(a);
+  if (ctx.gtile < 0) return;  // CTA-uniform: not a tile of the grid
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  int gx, gy0;
+  pixel_of2(ctx, t, gx, gy0);
+  const int gy1 = gy0 + 4;
+  const bool in0 = gx < ctx.width && gy0 < ctx.height;
+  const bool in1 = gx < ctx.width && gy1 < ctx.height;
+  const int s0 = a.start[ctx.gtile];
+  const int n = tile_list_length(a, ctx.gtile, s0);
+  if (n <= 0) return;
+  const float px = fmaf((float)gx, ctx.psx, ctx.topleft[0]);
+  const float py0 = fmaf((float)gy0, ctx.psy, ctx.topleft[1]);
+  const float py1 = fmaf((float)gy1, ctx.psy, ctx.topleft[1]);
+  P2Stage S;
+  S.wh = s_stage + warp * kP2StageWords;
+  S.wl = S.wh + 16 * kP2Cols;
+  S.yh = S.wl + 16 * kP2Cols;
+  S.yl = S.yh + 16 * kP2Cols;
+  int *slots = s_slots + warp * 8;
+  float2 Y2a[Sh<C>::NY2], Y2b[Sh<C>::NY2];
+  {
+    float Ya[CC], Yb[CC];
+    if constexpr (RGB) {
+      Ya[0] = 1.0f;
+      Yb[0] = 1.0f;
+    } else {
+      sh_basis<C>(ctx.c2w, px, py0, Ya);
+      sh_basis<C>(ctx.c2w, px, py1, Yb);
+    }
+    pack_basis<C>(Ya, Y2a);
+    pack_basis<C>(Yb, Y2b);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      uint32_t hi = 0u, lo = 0u;
+      if (k < CC) split_half2(Ya[k < CC ? k : 0], Yb[k < CC ? k : 0], hi, lo);
+      S.yh[p2_idx(k, lane)] = hi;
+      S.yl[p2_idx(k, lane)] = lo;
+      S.wh[p2_idx(k, lane)] = 0u;  // rows never staged stay finite
+      S.wl[p2_idx(k, lane)] = 0u;
+    }
+  }
+  // per-pixel state as (pixel A, pixel B) pairs
+  float2 fin2[3] = {f2(0.0f, 0.0f), f2(0.0f, 0.0f), f2(0.0f, 0.0f)};
+  float2 go2[3] = {f2(0.0f, 0.0f), f2(0.0f, 0.0f), f2(0.0f, 0.0f)};
+  if (in0) {
+    const int64_t pix = 3 * ((int64_t)gy0 * ctx.width + gx);
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+      fin2[ch].x = ctx.final_img[pix + ch];
+      go2[ch].x = ctx.grad_out[pix + ch];
+    }
+  }
+  if (in1) {
+    const int64_t pix = 3 * ((int64_t)gy1 * ctx.width + gx);
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+      fin2[ch].y = ctx.final_img[pix + ch];
+      go2[ch].y = ctx.grad_out[pix + ch];
+    }
+  }
+  float2 o[3] = {f2(0.0f, 0.0f), f2(0.0f, 0.0f), f2(0.0f, 0.0f)};
+  float2 T2 = f2(1.0f, 1.0f);
+  const float thr = a.T_thresh;
+  bool done0 = !in0, done1 = !in1;
+  float tx0, tx1, ty0, ty1;
+  tile_bounds(ctx, tx0, tx1, ty0, ty1);
+  const float4 blk = warp_block2(px, py0, py1);
+  if (t == 0 && sh_bulk_ok<C>(ctx.sh, ctx.sh_stride))
+    mbar_init(&s_bar);  // ordered before use by the loop's first barrier
+
+  for (int base = 0; base < n; base += B) {
+    if (__syncthreads_and(done0 && done1)) break;
+    const int nb = min(B, n - base);
+    for (int f = t; f < nb * NV; f += nthr) s_grad[f] = 0.0f;
+    for (int j = t; j < nb; j += nthr) s_touched[j] = 0;
+    const int nk = load_batch<C, true>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1,
+                                       s_wcount, &s_bar, (uint32_t)(base / B) & 1u);
+    if (nk < 0) return;  // flagged in g_raster_flags
+    const int nw = __all_sync(kFull, done0 && done1) ? 0 : warp_list(L, nk, blk, wl, lane);
+
+    int nslot = 0;  // warp-uniform: Gaussians staged in this warp's weight matrix
+    for (int j = 0; j < nw; ++j) {
+      const int i = wl[j];
+      if (__all_sync(kFull, done0 && done1)) break;
+      // a pixel stops before the Gaussian once its transmittance is below the
+      // threshold (the reference's per-Gaussian test)
+      if (!done0 && T2.x < thr) done0 = true;
+      if (!done1 && T2.y < thr) done1 = true;
+      bool c0 = false, c1 = false;
+      float G0 = 0.0f, G1 = 0.0f, tx_0 = 0.0f, ty_0 = 0.0f, tx_1 = 0.0f, ty_1 = 0.0f;
+      const float al = L.alpha[i];
+      const float4 cv = L.cov[i];
+      const float2 m = L.mean[i];
+      if (!(done0 && done1)) {
+        // both pixels' decision paths side by side, without branches: the
+        // radial of gs/src/include/kernels.h:172-187 (one det per Gaussian,
+        // IEEE division), then the exact exponential where it can decide
+        const float2 h = L.box[i];
+        const float x = px - m.x, y0 = py0 - m.y, y1 = py1 - m.y;
+        const float det = fmaf(cv.x, cv.w, -(cv.y * cv.z));
+        tx_0 = fmaf(x, cv.w, -(y0 * cv.z));
+        ty_0 = fmaf(-x, cv.y, y0 * cv.x);
+        tx_1 = fmaf(x, cv.w, -(y1 * cv.z));
+        ty_1 = fmaf(-x, cv.y, y1 * cv.x);
+        float r0 = fmaf(tx_0, x, ty_0 * y0) / det;
+        float r1 = fmaf(tx_1, x, ty_1 * y1) / det;
+        if (r0 < 0.0f) r0 = 1000.0f;
+        if (r1 < 0.0f) r1 = 1000.0f;
+        const bool xin = !(fabsf(x) > h.x);
+        const bool live0 = !done0 && xin && !(fabsf(y0) > h.y) && !surely_skipped(r0, al);
+        const bool live1 = !done1 && xin && !(fabsf(y1) > h.y) && !surely_skipped(r1, al);
+        // a live radial is NaN or in [0, 12]: -r/2 in [-6, 0] (NaN stays NaN)
+        float e0 = gsx_expf_neg(fmaxf(-0.5f * r0, -86.0f));
+        float e1 = gsx_expf_neg(fmaxf(-0.5f * r1, -86.0f));
+        if (r0 != r0) e0 = r0;
+        if (r1 != r1) e1 = r1;
+        c0 = live0 && !(al * e0 < kMinRenderAlpha);
+        c1 = live1 && !(al * e1 < kMinRenderAlpha);
+        G0 = c0 ? e0 : 0.0f;
+        G1 = c1 ? e1 : 0.0f;
+      }
+      float sc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+      float2 w[3] = {f2(0.0f, 0.0f), f2(0.0f, 0.0f), f2(0.0f, 0.0f)};
+      if (c0 || c1) {
+        // both pixels at once; a pixel that does not take this Gaussian has
+        // G = 0, so its colour sums and weights are unchanged / zero (its
+        // other terms are finite whenever the Gaussian's record is)
+        const float2 Gp = f2(G0, G1);
+        const float2 al2 = f2(al, al);
+        float2 coeff = __fmul2_rn(__fmul2_rn(al2, T2), Gp);
+        if (isnan(coeff.x)) coeff.x = 0.0f;
+        if (isnan(coeff.y)) coeff.y = 0.0f;
+        const float *s = L.sh + i * GSH;
+        float2 yv[3];
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+          if constexpr (RGB) {
+            const float v = fmaxf(s[ch * CCP], 0.0f);
+            yv[ch] = f2(v, v);
+          } else {
+            yv[ch] = f2(fmaxf(fast_sigmoid(sh_logit<C>(s + ch * CCP, Y2a)), 0.0f),  // NaN -> 0
+                        fmaxf(fast_sigmoid(sh_logit<C>(s + ch * CCP, Y2b)), 0.0f));
+          }
+          o[ch] = __ffma2_rn(coeff, yv[ch], o[ch]);
+        }
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+          if constexpr (RGB) {
+            w[ch] = __fmul2_rn(coeff, go2[ch]);
+          } else {
+            // y (1 - y), with 1 - y as fma(y, -1, 1)
+            const float2 yy = __fmul2_rn(yv[ch], __ffma2_rn(yv[ch], f2(-1.0f, -1.0f), f2(1.0f, 1.0f)));
+            w[ch] = __fmul2_rn(__fmul2_rn(coeff, yy), go2[ch]);
+          }
+        }
+        const float2 one_m = __ffma2_rn(f2(-al, -al), Gp, f2(1.0f, 1.0f));
+        float inv0, inv1;  // gradient path only: the hardware reciprocal (1 ulp)
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv0) : "f"(one_m.x));
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv1) : "f"(one_m.y));
+        const float2 inv_one_m = f2(inv0, inv1);
+        float2 P = f2(0.0f, 0.0f);
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+          // -q = (out - final) / (1 - aG): o - fin as fma(fin, -1, o), exact
+          const float2 nq = __fmul2_rn(__ffma2_rn(fin2[ch], f2(-1.0f, -1.0f), o[ch]), inv_one_m);
+          P = __ffma2_rn(go2[ch], __ffma2_rn(yv[ch], T2, nq), P);
+        }
+        const float2 dg = __fmul2_rn(__fmul2_rn(P, al2), Gp);
+        const float inv_det = L.inv_det[i];
+        const float2 idet = f2(inv_det, inv_det);
+        const float2 tmpx = __fmul2_rn(f2(tx_0, tx_1), idet);
+        const float2 tmpy = __fmul2_rn(f2(ty_0, ty_1), idet);
+        const float2 dx = __fmul2_rn(dg, tmpx), dy = __fmul2_rn(dg, tmpy);
+        const float2 s2 = __fmul2_rn(f2(0.5f, 0.5f), __fmul2_rn(dx, tmpx));
+        const float2 s3 = __fmul2_rn(f2(0.5f, 0.5f), __fmul2_rn(dx, tmpy));
+        const float2 s4 = __fmul2_rn(f2(0.5f, 0.5f), __fmul2_rn(dy, tmpy));
+        const float2 s5 = __fmul2_rn(P, Gp);
+        sc[0] = dx.x + dx.y;
+        sc[1] = dy.x + dy.y;
+        sc[2] = s2.x + s2.y;
+        sc[3] = s3.x + s3.y;
+        sc[4] = s4.x + s4.y;
+        sc[5] = s5.x + s5.y;
+        if (c0) T2.x = T2.x * one_m.x;
+        if (c1) T2.y = T2.y * one_m.y;
+      }
+      if (__ballot_sync(kFull, c0 || c1)) {
+        const float r = warp_sum6(sc, lane);
+        if ((lane & 3) == 0 && (lane >> 2) < 6 && r != 0.0f)
+          atomicAdd(&s_grad[i * NV + (lane >> 2)], r);
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+          uint32_t hi, lo;
+          split_half2(w[ch].x, w[ch].y, hi, lo);
+          S.wh[p2_idx(3 * nslot + ch, lane)] = hi;
+          S.wl[p2_idx(3 * nslot + ch, lane)] = lo;
+        }
+        if (lane == 0) {
+          slots[nslot] = i;
+          s_touched[i] = 1;
+        }
+        if (++nslot == kSlots) {
+          __syncwarp();
+          flush_sh_group2<C>(S, slots, nslot, s_grad, lane);
+          __syncwarp();
+          nslot = 0;
         }
       }
     }
+    if (nslot > 0) {
+      __syncwarp();
+      flush_sh_group2<C>(S, slots, nslot, s_grad, lane);
+      __syncwarp();
+    }
+    if (!done0 && T2.x < thr) done0 = true;
+    if (!done1 && T2.y < thr) done1 = true;
+    __syncthreads();
+    fold_batch_grads<C>(a, ctx, L, s_grad, s_touched, nk, t, nthr);
   }
 }
 
@@ -1095,8 +1470,57 @@ int launch_bwd_tt(RasterArgs a, int64_t grid, cudaStream_t s) {
   return cuda_status(cudaGetLastError(), "raster_backward_kernel launch");
 }
 
+// Gaussians per shared-memory batch of the two-pixel backward: with 128
+// threads per 16x16 tile, 40 keeps the CTA under 56 KB of shared memory, four
+// CTAs per SM.
+#ifndef GSX_BWD2_BATCH
+#define GSX_BWD2_BATCH 40
+#endif
+
+template <int C>
+size_t bwd2_smem(int B, int nthr) {
+  constexpr int NV = Grad<C>::NV;
+  const int nwarps = nthr / 32;
+  return (size_t)B * (kRecordFloats + Sh<C>::GSH + NV + 1) * sizeof(float) +
+         (size_t)nwarps * (kP2StageWords + 8 + B) * sizeof(uint32_t);
+}
+
+// The two-pixel backward covers tiles made of 8x8 blocks, up to 1024 pixels.
+inline bool two_pixel_tiles(const RasterArgs &a) {
+  return a.tile_w % 8 == 0 && a.tile_h % 8 == 0 && a.tile_w * a.tile_h <= 1024;
+}
+
+template <int C, int MAXT, bool BATCHED, bool RGB = false>
+int launch_bwd2_tt(RasterArgs a, int64_t grid, cudaStream_t s) {
+  const int nthr = a.tile_w * a.tile_h / 2;
+  a.vec_grads = ((reinterpret_cast<uintptr_t>(a.g_mean2d) & 7) == 0 &&
+                 (reinterpret_cast<uintptr_t>(a.g_cov2d) & 15) == 0)
+                    ? 1
+                    : 0;
+  a.batch = nthr < GSX_BWD2_BATCH ? nthr : GSX_BWD2_BATCH;
+  const size_t smem = bwd2_smem<C>(a.batch, nthr);
+  static size_t attr_done = 0;
+  cudaError_t e = ensure_smem(raster_backward2_kernel<C, MAXT, BATCHED, RGB>, smem, attr_done);
+  if (e != cudaSuccess) return cuda_status(e, "raster_backward2 smem attribute");
+  count_launches(1);
+  raster_backward2_kernel<C, MAXT, BATCHED, RGB><<<(unsigned)grid, nthr, smem, s>>>(a);
+  return cuda_status(cudaGetLastError(), "raster_backward2_kernel launch");
+}
+
+// Pixels per thread of the backward: a.pixels_per_thread 1 or 2, or 0 for
+// two wherever the tile is made of 8x8 blocks.
+inline bool use_two_pixels(const RasterArgs &a) {
+  return a.pixels_per_thread != 1 && two_pixel_tiles(a);
+}
+
 template <int C, bool BATCHED>
 int launch_bwd_t(const RasterArgs &a, int64_t grid, cudaStream_t s) {
+  if (use_two_pixels(a)) {
+    const int nthr = a.tile_w * a.tile_h / 2;
+    return nthr <= 128   ? launch_bwd2_tt<C, 128, BATCHED>(a, grid, s)
+           : nthr <= 256 ? launch_bwd2_tt<C, 256, BATCHED>(a, grid, s)
+                         : launch_bwd2_tt<C, 512, BATCHED>(a, grid, s);
+  }
   return block_threads(a) <= 256 ? launch_bwd_tt<C, 256, BATCHED>(a, grid, s)
                                  : launch_bwd_tt<C, 1024, BATCHED>(a, grid, s);
 }
@@ -1241,6 +1665,12 @@ int launch_raster_forward_rgb(const RasterArgs &a, cudaStream_t s) {
 int launch_raster_backward_rgb(const RasterArgs &a, cudaStream_t s) {
   const int64_t grid = (int64_t)a.n_tiles_w * a.n_tiles_h;
   if (grid == 0) return GSX_OK;
+  if (use_two_pixels(a)) {
+    const int nthr = a.tile_w * a.tile_h / 2;
+    return nthr <= 128   ? launch_bwd2_tt<1, 128, false, true>(a, grid, s)
+           : nthr <= 256 ? launch_bwd2_tt<1, 256, false, true>(a, grid, s)
+                         : launch_bwd2_tt<1, 512, false, true>(a, grid, s);
+  }
   return block_threads(a) <= 256 ? launch_bwd_tt<1, 256, false, true>(a, grid, s)
                                  : launch_bwd_tt<1, 1024, false, true>(a, grid, s);
 }

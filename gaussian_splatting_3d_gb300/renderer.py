@@ -92,6 +92,10 @@ class RasterSettings:
     # "ray" uses the true ray direction R (x, y, 1) (opt-in, not the
     # reference's images)
     sh_dir: str = "reference"
+    # raster backward schedule: pixels per thread (1, or 2 for tiles made of
+    # 8x8 blocks; 0 = 2 wherever it applies); the gradients agree within
+    # rounding, the choice is a matter of speed
+    pixels_per_thread: int = 0
 
     def grad_flags(self) -> int:
         if self.exact_grad:
@@ -261,6 +265,7 @@ def _raster_params(cam: CameraInfo, settings: RasterSettings, C: int, sh_stride:
     p.pixel_size_x, p.pixel_size_y = float(1.0 / cam.fx), float(1.0 / cam.fy)
     p.T_thresh = float(settings.T_thresh)
     p.write_empty_tiles = 1
+    p.pixels_per_thread = int(settings.pixels_per_thread)
     return p
 
 

@@ -42,8 +42,9 @@ const char *gsx_status_string(int status);
 /* Detail message of the last failing call on this host thread ("" if none). */
 const char *gsx_last_error(void);
 /* ABI version of this library (increments on any signature change). */
-/* 2: gsx_project_backward / gsx_batch_project_backward take grad_flags */
-#define GSX_ABI_VERSION 2
+/* 2: gsx_project_backward / gsx_batch_project_backward take grad_flags;
+   3: gsx_raster_params gains pixels_per_thread */
+#define GSX_ABI_VERSION 3
 int gsx_abi_version(void);
 /* Number of kernels this library has launched in this process so far. */
 uint64_t gsx_kernel_launch_count(void);
@@ -311,6 +312,10 @@ typedef struct gsx_raster_params {
   float pixel_size_x, pixel_size_y;
   float T_thresh;
   int32_t write_empty_tiles;    /* 1: write zeros for pixels of empty tiles */
+  int32_t pixels_per_thread;    /* raster backward schedule: pixels per thread,
+                                   1 or 2 (2 needs tile_w and tile_h multiples
+                                   of 8, else 1 is used); 0 = 2 wherever it
+                                   applies.  Results agree within rounding. */
 } gsx_raster_params;
 
 /* Forward raster over precomputed per-Gaussian mean2d/cov2d/alpha, SH

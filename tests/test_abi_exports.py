@@ -39,7 +39,7 @@ def test_python_binding_covers_header():
 
 def test_status_strings_and_host_validation_without_gpu():
     lib = _lib.load()
-    assert lib.gsx_abi_version() == _lib.GSX_ABI_VERSION == 2
+    assert lib.gsx_abi_version() == _lib.GSX_ABI_VERSION == 3
     assert lib.gsx_status_string(0) == b"ok"
     assert lib.gsx_status_string(2) == b"capacity exceeded"
     # argument validation happens on the host before any CUDA call

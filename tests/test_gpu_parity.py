@@ -150,6 +150,48 @@ def test_tile_shapes(tile):
     assert_image_close(got["image"], img)
 
 
+def oracle_rect_tiles(wl, tile_w, tile_h):
+    """The oracle pipeline (projection, binning, raster forward and backward,
+    projection backward) with tile_w x tile_h tiles."""
+    sc, view = wl.scene, wl.views[0]
+    cam = view.cam
+    from gaussian_splatting_3d_gb300.camera import frustum_np
+    normals, pts = frustum_np(view.c2w, cam)
+    ocam = O.make_camera(view.c2w, cam.fx, cam.fy, cam.cx, cam.cy, cam.w, cam.h, normals, pts)
+    pr = O.project(sc.mean, sc.qvec, sc.log_scale, sc.alpha_logit, ocam, 1.0, 6.0, tile_w, tile_h)
+    ntw, nth = (cam.w + tile_w - 1) // tile_w, (cam.h + tile_h - 1) // tile_h
+    b = O.bin_gaussians(pr["rect"], pr["rect"][:, 2:], pr["depth"], nth, ntw, stride=4)
+    P = O.raster_params(cam.w, cam.h, tile_w, tile_h, sc.sh_order, sc.sh.shape[-1])
+    tl = np.array(cam.topleft(), np.float32)
+    psx, psy = np.float32(1 / cam.fx), np.float32(1 / cam.fy)
+    img = O.render_fwd(P, pr["mean2d"], pr["cov2d"], sc.sh, pr["alpha"], b["start"], b["end"], b["ids"], tl,
+                       view.c2w, psx, psy)
+    g = O.render_bwd(P, pr["mean2d"], pr["cov2d"], sc.sh, pr["alpha"], b["start"], b["end"], b["ids"], tl,
+                     view.c2w, psx, psy, img, wl.grad_weight)
+    gp = O.project_bwd(sc.mean, sc.qvec, sc.log_scale, sc.alpha_logit, ocam, pr["mask"], g["mean2d"],
+                       g["cov2d"], g["alpha"])
+    gp["sh"] = g["sh"]
+    return img, gp
+
+
+@pytest.mark.parametrize("tile,ppt", [((16, 16), 1), ((16, 16), 2), ((8, 8), 2), ((32, 8), 2), ((16, 32), 2),
+                                      ((12, 12), 0), ((8, 8), 1)])
+@pytest.mark.parametrize("sh_degree", [0, 3])
+def test_backward_schedules_match_oracle(tile, ppt, sh_degree):
+    """Both raster backward schedules -- one pixel per thread, and two pixels
+    per thread over 8x8 warp blocks (tiles made of 8x8 blocks; a 12x12 tile
+    falls back to one) -- give the oracle's image and gradients."""
+    wl = S.custom_workload(4000, 96, 80, sh_degree, seed=11)
+    view = wl.views[0]
+    st = renderer.RasterSettings(tile_w=tile[0], tile_h=tile[1], pixels_per_thread=ppt)
+    got = gpu_pipeline(wl, st, with_grad=True)
+    img, ref = oracle_rect_tiles(wl, *tile)
+    assert_image_close(got["image"], img)
+    for k, g in got["grads"].items():
+        e = rel_err(g, ref[k])
+        assert e <= GRAD_REL, f"{k}: relative max error {e:.3g}"
+
+
 def test_dropin_gs_functions_match_oracle():
     """The reference-facing `_gs` entry points on the reference's own tensor
     layout (compacted visible Gaussians, separate [M,2] AABB corners)."""
