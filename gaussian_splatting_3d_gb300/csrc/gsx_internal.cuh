@@ -178,7 +178,7 @@ struct RasterArgs {
   // single view: CTA b renders tile tile_order[b] (a permutation of the tiles,
   // longest lists first); nullptr renders tile b
   const int32_t *tile_order;
-  // raster backward: 1 = one pixel per thread, 2 = two (tiles made of 8x8
+  // raster passes: 1 = one pixel per thread, 2 = two (tiles made of 8x8
   // blocks only), 0 = two wherever possible
   int32_t pixels_per_thread;
 };

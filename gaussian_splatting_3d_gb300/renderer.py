@@ -92,8 +92,9 @@ class RasterSettings:
     # "ray" uses the true ray direction R (x, y, 1) (opt-in, not the
     # reference's images)
     sh_dir: str = "reference"
-    # raster backward schedule: pixels per thread (1, or 2 for tiles made of
-    # 8x8 blocks; 0 = 2 wherever it applies); the gradients agree within
+    # raster schedule: pixels per thread (1, or 2 for tiles made of 8x8
+    # blocks; 0 = one for the forward and two for the backward, the faster
+    # measured choice); images are identical and gradients agree within
     # rounding, the choice is a matter of speed
     pixels_per_thread: int = 0
 

@@ -312,10 +312,13 @@ typedef struct gsx_raster_params {
   float pixel_size_x, pixel_size_y;
   float T_thresh;
   int32_t write_empty_tiles;    /* 1: write zeros for pixels of empty tiles */
-  int32_t pixels_per_thread;    /* raster backward schedule: pixels per thread,
-                                   1 or 2 (2 needs tile_w and tile_h multiples
-                                   of 8, else 1 is used); 0 = 2 wherever it
-                                   applies.  Results agree within rounding. */
+  int32_t pixels_per_thread;    /* raster schedule: pixels per thread, 1 or 2
+                                   (2 needs tile_w and tile_h multiples of 8,
+                                   else 1 is used; the forward with a
+                                   background or maps always uses 1); 0 = the
+                                   faster measured choice: 1 for the forward,
+                                   2 for the backward.  Images are identical,
+                                   gradients agree within rounding. */
 } gsx_raster_params;
 
 /* Forward raster over precomputed per-Gaussian mean2d/cov2d/alpha, SH

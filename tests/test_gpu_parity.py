@@ -190,6 +190,9 @@ def test_backward_schedules_match_oracle(tile, ppt, sh_degree):
     for k, g in got["grads"].items():
         e = rel_err(g, ref[k])
         assert e <= GRAD_REL, f"{k}: relative max error {e:.3g}"
+    # the forward's decisions and colour arithmetic do not depend on the schedule
+    other = renderer.RasterSettings(tile_w=tile[0], tile_h=tile[1], pixels_per_thread=1 if ppt != 1 else 2)
+    np.testing.assert_array_equal(gpu_pipeline(wl, other, with_grad=False)["image"], got["image"])
 
 
 def test_dropin_gs_functions_match_oracle():
