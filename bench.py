@@ -481,8 +481,8 @@ def run_batch(args):
     sc = B.Scene.from_arrays(wl.scene, dev)
     specs = [B.ViewSpec(0, v.c2w, v.cam) for v in wl.views]
     best, tune = B.autotune_tile([sc], specs, reps=1, device=dev)
-    st = renderer.RasterSettings(tile_w=best[0], tile_h=best[1])
-    bp = B.BatchPipeline(dev, st).plan([sc], specs)
+    st = renderer.RasterSettings(tile_w=best[0], tile_h=best[1], pixels_per_thread=best[2])
+    bp = B.BatchPipeline(dev, st, persistent=not args.no_persistent).plan([sc], specs)
     gen = torch.Generator(device="cpu").manual_seed(0)
     for g in bp.grad_outs:
         g.copy_(torch.rand(g.shape, generator=gen))
@@ -525,7 +525,8 @@ def run_batch(args):
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_batch, 3),
         "plain_per_view_views_per_s": round(V / (ms_plain * 1e-3), 2),
         "speedup_vs_plain": round(ms_plain / ms_batch, 3), "identical_images_first3": bool(same),
-        "tile": list(best), "autotune_ms": {f"{k[0]}x{k[1]}": round(v, 3) for k, v in tune.items()},
+        "tile": list(best[:2]), "pixels_per_thread": best[2], "persistent_raster": not args.no_persistent,
+        "autotune_ms": {f"{k[0]}x{k[1]}/ppt{k[2]}": round(v, 3) for k, v in tune.items()},
         "keys": int(bp.n_keys), "dtype": "f32", "data": "synthetic (seeded PCG64)",
         "config": {"workload": "batch: 32 views cycling 800x800/1280x720/1920x1080, SH degree 3, CUDA graph"},
     }
@@ -810,6 +811,8 @@ def main():
                     help="headline: SH colour per pixel (the reference) or per Gaussian (opt-in)")
     ap.add_argument("--pixels-per-thread", type=int, default=0, choices=[0, 1, 2],
                     help="raster backward schedule (0: two pixels per thread where the tile allows)")
+    ap.add_argument("--no-persistent", action="store_true",
+                    help="batch: one CTA per tile instead of persistent raster grids")
     ap.add_argument("--cpu-iters", type=int, default=5, help="whole CPU-oracle steps timed for cpu_baseline")
     args = ap.parse_args()
     if args.warmup < 3:

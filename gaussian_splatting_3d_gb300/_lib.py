@@ -149,8 +149,8 @@ SIGNATURES = {
     "gsx_batch_view_size": (c_size_t, []),
     "gsx_batch_project_forward": (c_int, [P, P, c_int32, c_float, c_float] + [P] * 7),
     "gsx_batch_bin_async": (c_int, [P, P, c_int32, P, P, P, c_int64, P, P, P, P, c_size_t, P]),
-    "gsx_batch_render_forward": (c_int, [P, P, c_int32, c_int64] + [P] * 6 + [c_float, P]),
-    "gsx_batch_render_backward": (c_int, [P, P, c_int32, c_int64] + [P] * 9 + [c_float, P]),
+    "gsx_batch_render_forward": (c_int, [P, P, c_int32, c_int64] + [P] * 6 + [c_float, P, P, P]),
+    "gsx_batch_render_backward": (c_int, [P, P, c_int32, c_int64] + [P] * 9 + [c_float, P, P, P]),
     "gsx_batch_project_backward": (c_int, [P, P, c_int32] + [P] * 4 + [c_int32, P]),
     # adaptive density control
     "gsx_densify_count_visible": (c_int, [c_int64, P, P, P]),

@@ -41,7 +41,7 @@ class GsxBatchView(ctypes.Structure):
         ("tile_w", c_int32), ("tile_h", c_int32), ("n_tiles_w", c_int32), ("n_tiles_h", c_int32),
         ("topleft", c_float * 2), ("pixel_size_x", c_float), ("pixel_size_y", c_float),
         ("out", c_void_p), ("grad_out", c_void_p),
-        ("write_empty_tiles", c_int32), ("reserved", c_int32),
+        ("write_empty_tiles", c_int32), ("pixels_per_thread", c_int32),
         ("cam", GsxCamera),
     ]
 
@@ -93,9 +93,14 @@ class ViewSpec:
 class BatchPipeline:
     """Plan once, then step (eager or graph replay) over a fixed set of views."""
 
-    def __init__(self, device=None, settings: RasterSettings | None = None):
+    def __init__(self, device=None, settings: RasterSettings | None = None, persistent: bool = True):
+        """persistent: the raster passes run as persistent grids that claim
+        the batch's tiles longest list first (gsx_tile_order + a work
+        counter); False launches one CTA per tile in index order.  Neither
+        choice changes an image or a gradient."""
         self.device = torch.device(device or "cuda")
         self.settings = settings or RasterSettings()
+        self.persistent = persistent
         self.graph = None
         self.key_capacity = 0
 
@@ -166,6 +171,7 @@ class BatchPipeline:
             e.pixel_size_x, e.pixel_size_y = float(1.0 / v.cam.fx), float(1.0 / v.cam.fy)
             e.out = ptr(self.images[i])
             e.write_empty_tiles = 1
+            e.pixels_per_thread = int(st.pixels_per_thread)
             e.cam = make_gsx_camera(v.c2w, v.cam)
             item += sc.n
             tile += ntw * nth
@@ -184,6 +190,8 @@ class BatchPipeline:
         self.counts = torch.empty((I,), dtype=torch.int32, device=dev)
         self.start = torch.empty((tile,), dtype=torch.int32, device=dev)
         self.end = torch.empty((tile,), dtype=torch.int32, device=dev)
+        self.order = torch.empty((tile,), dtype=torch.int32, device=dev)
+        self.work_counter = torch.zeros((4,), dtype=torch.int32, device=dev)
         if backward:
             self.g_mean2d = torch.zeros((I, 2), **f32)
             self.g_cov2d = torch.zeros((I, 4), **f32)
@@ -205,6 +213,13 @@ class BatchPipeline:
     def _views_args(self):
         return ptr(self.table_dev), ctypes.addressof(self.table), len(self.views)
 
+    def _queue_args(self):
+        """(tile_order, work_counter) of the raster passes: the order written
+        after the binning by forward_async, or none for index order."""
+        if not self.persistent:
+            return None, None
+        return ptr(self.order), ptr(self.work_counter)
+
     def forward_async(self):
         lib = _lib_batch()
         vd, vh, V = self._views_args()
@@ -217,9 +232,13 @@ class BatchPipeline:
         _lib.check(lib.gsx_batch_bin_async(vd, vh, V, ptr(self.rect), ptr(self.counts), ptr(self.depth),
                                            self.key_capacity, ptr(self.ids), ptr(self.start), ptr(self.end),
                                            ptr(self.ws), self.ws_bytes, s), "gsx_batch_bin_async")
+        if self.persistent:
+            _lib.check(lib.gsx_tile_order(ptr(self.start), ptr(self.end), self.n_tiles, ptr(self.order), s),
+                       "gsx_tile_order")
         _lib.check(lib.gsx_batch_render_forward(vd, vh, V, self.key_capacity, ptr(self.mean2d), ptr(self.cov2d),
                                                 ptr(self.alpha), ptr(self.start), ptr(self.end), ptr(self.ids),
-                                                float(st.T_thresh), s), "gsx_batch_render_forward")
+                                                float(st.T_thresh), *self._queue_args(), s),
+                   "gsx_batch_render_forward")
 
     def backward_async(self):
         lib = _lib_batch()
@@ -232,7 +251,8 @@ class BatchPipeline:
         _lib.check(lib.gsx_batch_render_backward(vd, vh, V, self.key_capacity, ptr(self.mean2d), ptr(self.cov2d),
                                                  ptr(self.alpha), ptr(self.start), ptr(self.end), ptr(self.ids),
                                                  ptr(self.g_mean2d), ptr(self.g_cov2d), ptr(self.g_alpha),
-                                                 float(self.settings.T_thresh), s), "gsx_batch_render_backward")
+                                                 float(self.settings.T_thresh), *self._queue_args(), s),
+                   "gsx_batch_render_backward")
         _lib.check(lib.gsx_batch_project_backward(vd, vh, V, ptr(self.counts), ptr(self.g_mean2d),
                                                   ptr(self.g_cov2d), ptr(self.g_alpha),
                                                   self.settings.grad_flags(), s),
@@ -303,24 +323,31 @@ class BatchPipeline:
 
 
 def autotune_tile(scenes, views, shapes=((8, 8), (16, 16), (32, 8)), base: RasterSettings | None = None,
-                  backward: bool = True, reps: int = 3, device=None):
-    """Time one batched step per tile shape and return (best shape, {shape: ms}).
-    The tile shape changes the AABB tile rectangles and therefore the images:
-    record the choice and keep it fixed when comparing runs."""
+                  backward: bool = True, reps: int = 3, device=None, schedules=(0, 1, 2)):
+    """Time one batched step per tile shape and raster schedule (pixels per
+    thread: 0 = one in the forward and two in the backward, 1, 2) and return
+    (best (tile_w, tile_h, pixels_per_thread), {that key: ms}).  The tile
+    shape changes the AABB tile rectangles and therefore the images: record
+    the choice and keep it fixed when comparing runs.  The schedule changes
+    no image (and the gradients only within rounding)."""
     base = base or RasterSettings()
     times = {}
     for tw, th in shapes:
-        st = RasterSettings(**{**base.__dict__, "tile_w": tw, "tile_h": th})
-        bp = BatchPipeline(device, st).plan(scenes, views, backward)
-        bp.step()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(reps):
+        bp = None
+        for ppt in schedules:
+            if ppt == 2 and (tw % 8 or th % 8):
+                continue  # two pixels per thread needs tiles made of 8x8 blocks
+            st = RasterSettings(**{**base.__dict__, "tile_w": tw, "tile_h": th, "pixels_per_thread": ppt})
+            bp = BatchPipeline(device, st).plan(scenes, views, backward)
             bp.step()
-        e1.record()
-        torch.cuda.synchronize()
-        times[(tw, th)] = e0.elapsed_time(e1) / reps
-        del bp
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                bp.step()
+            e1.record()
+            torch.cuda.synchronize()
+            times[(tw, th, ppt)] = e0.elapsed_time(e1) / reps
+            del bp
     best = min(times, key=times.get)
     return best, times

@@ -17,7 +17,7 @@ namespace {
 
 struct BatchShape {
   int64_t n_items = 0, total_tiles = 0, max_n = 0;
-  int32_t tile_w = 0, tile_h = 0, sh_order = 0;
+  int32_t tile_w = 0, tile_h = 0, sh_order = 0, pixels_per_thread = 0;
   bool one_scene = true;
 };
 
@@ -29,10 +29,17 @@ int check_views(const gsx_batch_view *hv, int32_t n_views, BatchShape &b) {
   b.tile_w = hv[0].tile_w;
   b.tile_h = hv[0].tile_h;
   b.sh_order = hv[0].sh_order;
+  b.pixels_per_thread = hv[0].pixels_per_thread;
   for (int32_t i = 0; i < n_views; ++i) {
     const gsx_batch_view &v = hv[i];
-    if (v.tile_w != b.tile_w || v.tile_h != b.tile_h || v.sh_order != b.sh_order) {
-      set_error("view %d: all views of a batch share the tile shape and SH order", i);
+    if (v.tile_w != b.tile_w || v.tile_h != b.tile_h || v.sh_order != b.sh_order ||
+        v.pixels_per_thread != hv[0].pixels_per_thread) {
+      set_error("view %d: all views of a batch share the tile shape, SH order and raster schedule",
+                i);
+      return GSX_ERR_INVALID_ARG;
+    }
+    if (v.pixels_per_thread < 0 || v.pixels_per_thread > 2) {
+      set_error("view %d: pixels_per_thread must be 0, 1 or 2 (got %d)", i, v.pixels_per_thread);
       return GSX_ERR_INVALID_ARG;
     }
     if (v.item_offset != b.n_items || v.tile_offset != b.total_tiles) {
@@ -90,6 +97,7 @@ RasterArgs batch_args(const gsx_batch_view *dv, int32_t n_views, const BatchShap
   a.ids = ids;
   a.views = dv;
   a.n_views = n_views;
+  a.pixels_per_thread = b.pixels_per_thread;
   return a;
 }
 
@@ -143,7 +151,7 @@ int gsx_batch_render_forward(const gsx_batch_view *views_dev, const gsx_batch_vi
                              int32_t n_views, int64_t key_capacity, const float *mean2d,
                              const float *cov2d, const float *alpha, const int32_t *start,
                              const int32_t *end, const int32_t *gaussian_ids, float T_thresh,
-                             void *stream) {
+                             const int32_t *tile_order, uint32_t *work_counter, void *stream) {
   BatchShape b;
   int st = check_views(views_host, n_views, b);
   if (st != GSX_OK) return st;
@@ -159,6 +167,8 @@ int gsx_batch_render_forward(const gsx_batch_view *views_dev, const gsx_batch_vi
   }
   RasterArgs a = batch_args(views_dev, n_views, b, key_capacity, mean2d, cov2d, alpha, start, end,
                             gaussian_ids, T_thresh);
+  a.tile_order = tile_order;
+  a.work_counter = work_counter;
   return launch_raster_forward_batch(a, b.sh_order, b.total_tiles, as_stream(stream));
 }
 
@@ -166,7 +176,8 @@ int gsx_batch_render_backward(const gsx_batch_view *views_dev, const gsx_batch_v
                               int32_t n_views, int64_t key_capacity, const float *mean2d,
                               const float *cov2d, const float *alpha, const int32_t *start,
                               const int32_t *end, const int32_t *gaussian_ids, float *g_mean2d,
-                              float *g_cov2d, float *g_alpha, float T_thresh, void *stream) {
+                              float *g_cov2d, float *g_alpha, float T_thresh,
+                              const int32_t *tile_order, uint32_t *work_counter, void *stream) {
   BatchShape b;
   int st = check_views(views_host, n_views, b);
   if (st != GSX_OK) return st;
@@ -185,6 +196,8 @@ int gsx_batch_render_backward(const gsx_batch_view *views_dev, const gsx_batch_v
   a.g_mean2d = g_mean2d;
   a.g_cov2d = g_cov2d;
   a.g_alpha = g_alpha;
+  a.tile_order = tile_order;
+  a.work_counter = work_counter;
   return launch_raster_backward_batch(a, b.sh_order, b.total_tiles, as_stream(stream));
 }
 

@@ -181,6 +181,11 @@ struct RasterArgs {
   // raster passes: 1 = one pixel per thread, 2 = two (tiles made of 8x8
   // blocks only), 0 = two wherever possible
   int32_t pixels_per_thread;
+  // work items (tiles) of the launch, set by the launcher; with work_counter
+  // (a zeroed device word) the grid is persistent: resident CTAs claim the
+  // items (tile_order[item] when given) one atomic at a time
+  int64_t n_work;
+  uint32_t *work_counter;
 };
 int launch_raster_forward(const RasterArgs &a, int C, cudaStream_t s);
 // order[0..n_tiles) = the tiles by descending list length (end - start), in

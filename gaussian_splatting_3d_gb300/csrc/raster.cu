@@ -160,15 +160,30 @@ struct ViewCtx {
   int write_empty;
 };
 
+// Work items of a raster launch: one per tile.  Without a work counter CTA b
+// takes item b; with one (a persistent grid of resident CTAs) every CTA
+// claims items in turn through one atomic each, until a.n_work are taken.
+// Returns -1 when the CTA has no further item.  CTA-uniform.
+template <bool PERSIST>
+__device__ __forceinline__ int64_t claim_work(const RasterArgs &a, int *s_work, bool first) {
+  if constexpr (!PERSIST) return first ? (int64_t)blockIdx.x : -1;
+  __syncthreads();  // the previous tile's shared memory is no longer read
+  if (threadIdx.x == 0) *s_work = (int)atomicAdd(a.work_counter, 1u);
+  __syncthreads();
+  const int64_t w = *s_work;
+  return w < a.n_work ? w : -1;
+}
+
+// The tile of work item `work`: tile_order[work] (longest lists first) or the
+// item itself; an entry outside [0, n_work) renders nothing (gtile = -1).
 template <bool BATCHED>
-__device__ __forceinline__ ViewCtx make_ctx(const RasterArgs &a) {
+__device__ __forceinline__ ViewCtx make_ctx(const RasterArgs &a, int64_t work) {
   ViewCtx c;
-  c.gtile = blockIdx.x;
+  int64_t g = a.tile_order ? (int64_t)a.tile_order[work] : work;
+  if (g < 0 || g >= a.n_work) g = -1;
+  c.gtile = (int)g;
+  if (g < 0) return c;
   if constexpr (!BATCHED) {
-    if (a.tile_order) {  // an entry outside the grid renders nothing (gtile = -1)
-      const int g = a.tile_order[blockIdx.x];
-      c.gtile = (g >= 0 && g < (int)gridDim.x) ? g : -1;
-    }
     c.tile = c.gtile;
     c.n_tiles_w = a.n_tiles_w;
     c.tile_w = a.tile_w;
@@ -189,7 +204,7 @@ __device__ __forceinline__ ViewCtx make_ctx(const RasterArgs &a) {
     c.g_sh = a.g_sh;
     c.write_empty = a.write_empty;
   } else {
-    const int64_t gt = blockIdx.x;
+    const int64_t gt = g;
     int lo = 0, hi = a.n_views - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
@@ -582,128 +597,145 @@ __device__ __forceinline__ void pack_basis(const float *Y, float2 *Y2) {
 // RGB: per-Gaussian colours (an opt-in mode; the reference evaluates SH per
 // pixel): `sh` holds rgb [n,3] as C = 1 rows, the basis is the constant 1
 // and the colour is the stored value itself.
-template <int C, int MAXT, bool BATCHED, bool EXTRAS, bool RGB = false>
+template <int C, int MAXT, bool BATCHED, bool EXTRAS, bool RGB = false, bool PERSIST = false>
 __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a) {
   constexpr int GSH = Sh<C>::GSH, CCP = Sh<C>::CCP;
   extern __shared__ float4 smem4[];
   __shared__ int s_wcount[32];
   __shared__ uint64_t s_bar;  // bulk-copy barrier of the SH rows
+  __shared__ int s_work;
   const int nthr = blockDim.x;
   const int B = a.batch;
   SmemLayout L = carve<C>(reinterpret_cast<float *>(smem4), B);
   int *wl = reinterpret_cast<int *>(L.sh + B * GSH) + (threadIdx.x >> 5) * B;  // [nwarps][B]
 
-  const ViewCtx ctx = make_ctx<BATCHED>(a);
-  if (ctx.gtile < 0) return;  // CTA-uniform: not a tile of the grid
-  const int t = threadIdx.x, lane = t & 31;
-  int gx, gy;
-  pixel_of(ctx, t, gx, gy);
-  const bool inside = t < ctx.tile_w * ctx.tile_h && gx < ctx.width && gy < ctx.height;
-  const int s0 = a.start[ctx.gtile];
-  const int n = tile_list_length(a, ctx.gtile, s0);
-  if (n <= 0) {
-    if (ctx.write_empty && inside) {
-      const int64_t pix = (int64_t)gy * ctx.width + gx;
-      float *dst = ctx.out + 3 * pix;
-      const bool bg = EXTRAS && a.has_bg;
-      dst[0] = bg ? a.bg[0] : 0.0f;
-      dst[1] = bg ? a.bg[1] : 0.0f;
-      dst[2] = bg ? a.bg[2] : 0.0f;
-      if constexpr (EXTRAS) {
-        if (a.alpha_out) a.alpha_out[pix] = 0.0f;
-        if (a.depth_out) a.depth_out[pix] = 0.0f;
-      }
-    }
-    return;
-  }
-  const float px = fmaf((float)gx, ctx.psx, ctx.topleft[0]);
-  const float py = fmaf((float)gy, ctx.psy, ctx.topleft[1]);
-  float2 Y2[Sh<C>::NY2];
-  {
-    float Y[Sh<C>::CC];
-    if constexpr (RGB) Y[0] = 1.0f;
-    else sh_basis<C>(ctx.c2w, px, py, Y);
-    pack_basis<C>(Y, Y2);
-  }
-  float o0 = 0.0f, o1 = 0.0f, o2 = 0.0f, T = 1.0f, dsum = 0.0f;
-  const bool want_depth = EXTRAS && a.depth_out != nullptr;
-  const float thr = a.T_thresh;
-  bool done = !inside;
-  float tx0, tx1, ty0, ty1;
-  tile_bounds(ctx, tx0, tx1, ty0, ty1);
-  const float4 blk = warp_block(px, py);
-  if (t == 0 && sh_bulk_ok<C>(ctx.sh, ctx.sh_stride))
-    mbar_init(&s_bar);  // ordered before use by the loop's first barrier
-
-  for (int base = 0; base < n; base += B) {
-    if (__syncthreads_and(done)) break;
-    const int nb = min(B, n - base);
-    const int nk = load_batch<C, false, EXTRAS>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0,
-                                                ty1, s_wcount, &s_bar, (uint32_t)(base / B) & 1u);
-    if (nk < 0) return;  // flagged in g_raster_flags
-    const int nw = __all_sync(kFull, done) ? 0 : warp_list(L, nk, blk, wl, lane);
-    if (!done) {
-      for (int j = 0; j < nw; ++j) {
-        const int i = wl[j];
-        if (T < thr) {
-          done = true;
-          break;
-        }
-        const float2 m = L.mean[i];
-        const float2 h = L.box[i];
-        const float x = px - m.x, y = py - m.y;
-        if (fabsf(x) > h.x || fabsf(y) > h.y) continue;
-        const float al = L.alpha[i];
-        const float radial = radial_of(L.cov[i], x, y);
-        if (surely_skipped(radial, al)) continue;
-        const float G = gsx_expf(-0.5f * radial);
-        float coeff = al * T;
-        coeff = coeff * G;
-        if (al * G < kMinRenderAlpha) continue;
-        if (isnan(coeff)) coeff = 0.0f;
-        const float *s = L.sh + i * GSH;
-        float y0, y1, y2;
-        if constexpr (RGB) {
-          y0 = s[0];
-          y1 = s[CCP];
-          y2 = s[2 * CCP];
-        } else {
-          y0 = fast_sigmoid(sh_logit<C>(s, Y2));
-          y1 = fast_sigmoid(sh_logit<C>(s + CCP, Y2));
-          y2 = fast_sigmoid(sh_logit<C>(s + 2 * CCP, Y2));
-        }
-        // coeff is finite here, so y * coeff is NaN exactly when y is; fmaxf
-        // returns its non-NaN operand and y >= 0, so this is the reference's
-        // `if isnan(y * coeff) y = 0`
-        y0 = fmaxf(y0, 0.0f);
-        y1 = fmaxf(y1, 0.0f);
-        y2 = fmaxf(y2, 0.0f);
-        o0 = fmaf(coeff, y0, o0);
-        o1 = fmaf(coeff, y1, o1);
-        o2 = fmaf(coeff, y2, o2);
+  if (PERSIST && threadIdx.x == 0) mbar_init(&s_bar);  // once per CTA, before any tile's first wait
+  // bulk-copy phases completed by this CTA: the barrier's parity across the
+  // tiles of a persistent grid (one tile per CTA: the batch index's parity)
+  uint32_t nphase = 0;
+  // one tile; false when the CTA must stop (a bulk-copy wait gave up)
+  auto run_tile = [&](int64_t work) -> bool {
+    const ViewCtx ctx = make_ctx<BATCHED>(a, work);
+    if (ctx.gtile < 0) return true;  // CTA-uniform: not a tile of the grid
+    if (!PERSIST && threadIdx.x == 0 && sh_bulk_ok<C>(ctx.sh, ctx.sh_stride))
+      mbar_init(&s_bar);  // ordered before use by the batch loop's first barrier
+    const int t = threadIdx.x, lane = t & 31;
+    int gx, gy;
+    pixel_of(ctx, t, gx, gy);
+    const bool inside = t < ctx.tile_w * ctx.tile_h && gx < ctx.width && gy < ctx.height;
+    const int s0 = a.start[ctx.gtile];
+    const int n = tile_list_length(a, ctx.gtile, s0);
+    if (n <= 0) {
+      if (ctx.write_empty && inside) {
+        const int64_t pix = (int64_t)gy * ctx.width + gx;
+        float *dst = ctx.out + 3 * pix;
+        const bool bg = EXTRAS && a.has_bg;
+        dst[0] = bg ? a.bg[0] : 0.0f;
+        dst[1] = bg ? a.bg[1] : 0.0f;
+        dst[2] = bg ? a.bg[2] : 0.0f;
         if constexpr (EXTRAS) {
-          if (want_depth) dsum = fmaf(coeff, L.zdep[i], dsum);
+          if (a.alpha_out) a.alpha_out[pix] = 0.0f;
+          if (a.depth_out) a.depth_out[pix] = 0.0f;
         }
-        T = T * fmaf(-al, G, 1.0f);
       }
-      if (T < thr) done = true;
+      return true;
     }
-  }
-  if (inside) {
-    const int64_t pix = (int64_t)gy * ctx.width + gx;
-    if (EXTRAS && a.has_bg) {  // what the Gaussians leave of the ray sees the background
-      o0 = fmaf(T, a.bg[0], o0);
-      o1 = fmaf(T, a.bg[1], o1);
-      o2 = fmaf(T, a.bg[2], o2);
+    const float px = fmaf((float)gx, ctx.psx, ctx.topleft[0]);
+    const float py = fmaf((float)gy, ctx.psy, ctx.topleft[1]);
+    float2 Y2[Sh<C>::NY2];
+    {
+      float Y[Sh<C>::CC];
+      if constexpr (RGB) Y[0] = 1.0f;
+      else sh_basis<C>(ctx.c2w, px, py, Y);
+      pack_basis<C>(Y, Y2);
     }
-    float *dst = ctx.out + 3 * pix;
-    dst[0] = o0;
-    dst[1] = o1;
-    dst[2] = o2;
-    if constexpr (EXTRAS) {
-      if (a.alpha_out) a.alpha_out[pix] = 1.0f - T;
-      if (want_depth) a.depth_out[pix] = dsum;
+    float o0 = 0.0f, o1 = 0.0f, o2 = 0.0f, T = 1.0f, dsum = 0.0f;
+    const bool want_depth = EXTRAS && a.depth_out != nullptr;
+    const float thr = a.T_thresh;
+    bool done = !inside;
+    float tx0, tx1, ty0, ty1;
+    tile_bounds(ctx, tx0, tx1, ty0, ty1);
+    const float4 blk = warp_block(px, py);
+
+    for (int base = 0; base < n; base += B) {
+      if (__syncthreads_and(done)) break;
+      const int nb = min(B, n - base);
+      const int nk = load_batch<C, false, EXTRAS>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0,
+                                                  ty1, s_wcount, &s_bar, PERSIST ? (nphase & 1u) : ((uint32_t)(base / B) & 1u));
+      if (nk < 0) return false;  // flagged in g_raster_flags
+      if (PERSIST && sh_bulk_ok<C>(ctx.sh, ctx.sh_stride)) ++nphase;
+      const int nw = __all_sync(kFull, done) ? 0 : warp_list(L, nk, blk, wl, lane);
+      if (!done) {
+        for (int j = 0; j < nw; ++j) {
+          const int i = wl[j];
+          if (T < thr) {
+            done = true;
+            break;
+          }
+          const float2 m = L.mean[i];
+          const float2 h = L.box[i];
+          const float x = px - m.x, y = py - m.y;
+          if (fabsf(x) > h.x || fabsf(y) > h.y) continue;
+          const float al = L.alpha[i];
+          const float radial = radial_of(L.cov[i], x, y);
+          if (surely_skipped(radial, al)) continue;
+          const float G = gsx_expf(-0.5f * radial);
+          float coeff = al * T;
+          coeff = coeff * G;
+          if (al * G < kMinRenderAlpha) continue;
+          if (isnan(coeff)) coeff = 0.0f;
+          const float *s = L.sh + i * GSH;
+          float y0, y1, y2;
+          if constexpr (RGB) {
+            y0 = s[0];
+            y1 = s[CCP];
+            y2 = s[2 * CCP];
+          } else {
+            y0 = fast_sigmoid(sh_logit<C>(s, Y2));
+            y1 = fast_sigmoid(sh_logit<C>(s + CCP, Y2));
+            y2 = fast_sigmoid(sh_logit<C>(s + 2 * CCP, Y2));
+          }
+          // coeff is finite here, so y * coeff is NaN exactly when y is; fmaxf
+          // returns its non-NaN operand and y >= 0, so this is the reference's
+          // `if isnan(y * coeff) y = 0`
+          y0 = fmaxf(y0, 0.0f);
+          y1 = fmaxf(y1, 0.0f);
+          y2 = fmaxf(y2, 0.0f);
+          o0 = fmaf(coeff, y0, o0);
+          o1 = fmaf(coeff, y1, o1);
+          o2 = fmaf(coeff, y2, o2);
+          if constexpr (EXTRAS) {
+            if (want_depth) dsum = fmaf(coeff, L.zdep[i], dsum);
+          }
+          T = T * fmaf(-al, G, 1.0f);
+        }
+        if (T < thr) done = true;
+      }
     }
+    if (inside) {
+      const int64_t pix = (int64_t)gy * ctx.width + gx;
+      if (EXTRAS && a.has_bg) {  // what the Gaussians leave of the ray sees the background
+        o0 = fmaf(T, a.bg[0], o0);
+        o1 = fmaf(T, a.bg[1], o1);
+        o2 = fmaf(T, a.bg[2], o2);
+      }
+      float *dst = ctx.out + 3 * pix;
+      dst[0] = o0;
+      dst[1] = o1;
+      dst[2] = o2;
+      if constexpr (EXTRAS) {
+        if (a.alpha_out) a.alpha_out[pix] = 1.0f - T;
+        if (want_depth) a.depth_out[pix] = dsum;
+      }
+    }
+    return true;
+  };
+  if constexpr (PERSIST) {
+    for (int64_t work = claim_work<true>(a, &s_work, true); work >= 0;
+         work = claim_work<true>(a, &s_work, false))
+      if (!run_tile(work)) return;
+  } else {
+    run_tile(blockIdx.x);
   }
 }
 
@@ -876,7 +908,7 @@ __device__ __forceinline__ void fold_batch_grads(const RasterArgs &a, const View
 
 // RGB: as in the forward; the gradient staged for the C = 1 reduction is
 // then dL/drgb itself (the constant basis makes the product a plain sum).
-template <int C, int MAXT, bool BATCHED, bool RGB = false>
+template <int C, int MAXT, bool BATCHED, bool RGB = false, bool PERSIST = false>
 __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1)
     raster_backward_kernel(const RasterArgs a) {
   constexpr int CC = Sh<C>::CC, CCP = Sh<C>::CCP, GSH = Sh<C>::GSH;
@@ -884,6 +916,7 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
   extern __shared__ float4 smem4[];
   __shared__ int s_wcount[32];
   __shared__ uint64_t s_bar;  // bulk-copy barrier of the SH rows
+  __shared__ int s_work;
   float *smem = reinterpret_cast<float *>(smem4);
   const int B = a.batch;
   const int nthr = blockDim.x, nwarps = nthr >> 5;
@@ -895,144 +928,160 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
   int *s_touched = s_slots + nwarps * 8;                                  // [B]
   int *wl = s_touched + B + (threadIdx.x >> 5) * B;                       // [nwarps][B]
 
-  const ViewCtx ctx = make_ctx<BATCHED>(a);
-  if (ctx.gtile < 0) return;  // CTA-uniform: not a tile of the grid
-  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  int gx, gy;
-  pixel_of(ctx, t, gx, gy);
-  const bool inside = t < ctx.tile_w * ctx.tile_h && gx < ctx.width && gy < ctx.height;
-  const int s0 = a.start[ctx.gtile];
-  const int n = tile_list_length(a, ctx.gtile, s0);
-  if (n <= 0) return;
-  const float px = fmaf((float)gx, ctx.psx, ctx.topleft[0]);
-  const float py = fmaf((float)gy, ctx.psy, ctx.topleft[1]);
-  float2 Y2[Sh<C>::NY2];
-  float *Ws = s_w + warp * 16 * kWStride;
-  float *Ys = s_y + warp * 16 * kYStride;
-  int *slots = s_slots + warp * 8;
-  {
-    float Y[CC];
-    if constexpr (RGB) Y[0] = 1.0f;
-    else sh_basis<C>(ctx.c2w, px, py, Y);
-    pack_basis<C>(Y, Y2);
-#pragma unroll
-    for (int k = 0; k < 16; ++k) Ys[k * kYStride + lane] = k < CC ? Y[k < CC ? k : 0] : 0.0f;
-  }
-  float fin[3] = {0.0f, 0.0f, 0.0f}, go[3] = {0.0f, 0.0f, 0.0f};
-  if (inside) {
-    const int64_t pix = 3 * ((int64_t)gy * ctx.width + gx);
-#pragma unroll
-    for (int ch = 0; ch < 3; ++ch) {
-      fin[ch] = ctx.final_img[pix + ch];
-      go[ch] = ctx.grad_out[pix + ch];
+  if (PERSIST && threadIdx.x == 0) mbar_init(&s_bar);  // once per CTA, before any tile's first wait
+  // bulk-copy phases completed by this CTA: the barrier's parity across the
+  // tiles of a persistent grid (one tile per CTA: the batch index's parity)
+  uint32_t nphase = 0;
+  // one tile; false when the CTA must stop (a bulk-copy wait gave up)
+  auto run_tile = [&](int64_t work) -> bool {
+    const ViewCtx ctx = make_ctx<BATCHED>(a, work);
+    if (ctx.gtile < 0) return true;  // CTA-uniform: not a tile of the grid
+    if (!PERSIST && threadIdx.x == 0 && sh_bulk_ok<C>(ctx.sh, ctx.sh_stride))
+      mbar_init(&s_bar);  // ordered before use by the batch loop's first barrier
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    int gx, gy;
+    pixel_of(ctx, t, gx, gy);
+    const bool inside = t < ctx.tile_w * ctx.tile_h && gx < ctx.width && gy < ctx.height;
+    const int s0 = a.start[ctx.gtile];
+    const int n = tile_list_length(a, ctx.gtile, s0);
+    if (n <= 0) return true;
+    const float px = fmaf((float)gx, ctx.psx, ctx.topleft[0]);
+    const float py = fmaf((float)gy, ctx.psy, ctx.topleft[1]);
+    float2 Y2[Sh<C>::NY2];
+    float *Ws = s_w + warp * 16 * kWStride;
+    float *Ys = s_y + warp * 16 * kYStride;
+    int *slots = s_slots + warp * 8;
+    {
+      float Y[CC];
+      if constexpr (RGB) Y[0] = 1.0f;
+      else sh_basis<C>(ctx.c2w, px, py, Y);
+      pack_basis<C>(Y, Y2);
+  #pragma unroll
+      for (int k = 0; k < 16; ++k) Ys[k * kYStride + lane] = k < CC ? Y[k < CC ? k : 0] : 0.0f;
     }
-  }
-  float o[3] = {0.0f, 0.0f, 0.0f};
-  float T = 1.0f;
-  const float thr = a.T_thresh;
-  bool done = !inside;
-  float tx0, tx1, ty0, ty1;
-  tile_bounds(ctx, tx0, tx1, ty0, ty1);
-  const float4 blk = warp_block(px, py);
-  if (t == 0 && sh_bulk_ok<C>(ctx.sh, ctx.sh_stride))
-    mbar_init(&s_bar);  // ordered before use by the loop's first barrier
+    float fin[3] = {0.0f, 0.0f, 0.0f}, go[3] = {0.0f, 0.0f, 0.0f};
+    if (inside) {
+      const int64_t pix = 3 * ((int64_t)gy * ctx.width + gx);
+  #pragma unroll
+      for (int ch = 0; ch < 3; ++ch) {
+        fin[ch] = ctx.final_img[pix + ch];
+        go[ch] = ctx.grad_out[pix + ch];
+      }
+    }
+    float o[3] = {0.0f, 0.0f, 0.0f};
+    float T = 1.0f;
+    const float thr = a.T_thresh;
+    bool done = !inside;
+    float tx0, tx1, ty0, ty1;
+    tile_bounds(ctx, tx0, tx1, ty0, ty1);
+    const float4 blk = warp_block(px, py);
 
-  for (int base = 0; base < n; base += B) {
-    if (__syncthreads_and(done)) break;
-    const int nb = min(B, n - base);
-    for (int f = t; f < nb * NV; f += nthr) s_grad[f] = 0.0f;
-    for (int j = t; j < nb; j += nthr) s_touched[j] = 0;
-    const int nk = load_batch<C, true>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1,
-                                       s_wcount, &s_bar, (uint32_t)(base / B) & 1u);
-    if (nk < 0) return;  // flagged in g_raster_flags
-    const int nw = __all_sync(kFull, done) ? 0 : warp_list(L, nk, blk, wl, lane);
+    for (int base = 0; base < n; base += B) {
+      if (__syncthreads_and(done)) break;
+      const int nb = min(B, n - base);
+      for (int f = t; f < nb * NV; f += nthr) s_grad[f] = 0.0f;
+      for (int j = t; j < nb; j += nthr) s_touched[j] = 0;
+      const int nk = load_batch<C, true>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1,
+                                         s_wcount, &s_bar, PERSIST ? (nphase & 1u) : ((uint32_t)(base / B) & 1u));
+      if (nk < 0) return false;  // flagged in g_raster_flags
+      if (PERSIST && sh_bulk_ok<C>(ctx.sh, ctx.sh_stride)) ++nphase;
+      const int nw = __all_sync(kFull, done) ? 0 : warp_list(L, nk, blk, wl, lane);
 
-    int nslot = 0;  // warp-uniform: Gaussians staged in this warp's weight matrix
-    for (int j = 0; j < nw; ++j) {
-      const int i = wl[j];
-      if (__all_sync(kFull, done)) break;
-      bool contrib = false;
-      float sc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-      float w[3] = {0.0f, 0.0f, 0.0f};
-      if (!done) {
-        if (T < thr) {
-          done = true;
-        } else {
-          const float al = L.alpha[i];
-          const float4 cv = L.cov[i];
-          const float2 m = L.mean[i];
-          const float2 h = L.box[i];
-          const float x = px - m.x, yy = py - m.y;
-          const bool outside = fabsf(x) > h.x || fabsf(yy) > h.y;
-          const float radial = outside ? 0.0f : radial_of(cv, x, yy);
-          if (!outside && !surely_skipped(radial, al)) {
-            const float G = gsx_expf(-0.5f * radial);
-            if (!(al * G < kMinRenderAlpha)) {
-              contrib = true;
-              float coeff = al * T * G;
-              if (isnan(coeff)) coeff = 0.0f;
-              const float *s = L.sh + i * GSH;
-              float y[3];
-#pragma unroll
-              for (int ch = 0; ch < 3; ++ch) {
-                y[ch] = RGB ? fmaxf(s[ch * CCP], 0.0f)
-                            : fmaxf(fast_sigmoid(sh_logit<C>(s + ch * CCP, Y2)), 0.0f);  // NaN -> 0
-                o[ch] = fmaf(coeff, y[ch], o[ch]);
+      int nslot = 0;  // warp-uniform: Gaussians staged in this warp's weight matrix
+      for (int j = 0; j < nw; ++j) {
+        const int i = wl[j];
+        if (__all_sync(kFull, done)) break;
+        bool contrib = false;
+        float sc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        float w[3] = {0.0f, 0.0f, 0.0f};
+        if (!done) {
+          if (T < thr) {
+            done = true;
+          } else {
+            const float al = L.alpha[i];
+            const float4 cv = L.cov[i];
+            const float2 m = L.mean[i];
+            const float2 h = L.box[i];
+            const float x = px - m.x, yy = py - m.y;
+            const bool outside = fabsf(x) > h.x || fabsf(yy) > h.y;
+            const float radial = outside ? 0.0f : radial_of(cv, x, yy);
+            if (!outside && !surely_skipped(radial, al)) {
+              const float G = gsx_expf(-0.5f * radial);
+              if (!(al * G < kMinRenderAlpha)) {
+                contrib = true;
+                float coeff = al * T * G;
+                if (isnan(coeff)) coeff = 0.0f;
+                const float *s = L.sh + i * GSH;
+                float y[3];
+  #pragma unroll
+                for (int ch = 0; ch < 3; ++ch) {
+                  y[ch] = RGB ? fmaxf(s[ch * CCP], 0.0f)
+                              : fmaxf(fast_sigmoid(sh_logit<C>(s + ch * CCP, Y2)), 0.0f);  // NaN -> 0
+                  o[ch] = fmaf(coeff, y[ch], o[ch]);
+                }
+  #pragma unroll
+                for (int ch = 0; ch < 3; ++ch)
+                  w[ch] = RGB ? coeff * go[ch] : coeff * (y[ch] * (1.0f - y[ch])) * go[ch];
+                const float one_m = fmaf(-al, G, 1.0f);
+                float inv_one_m;  // gradient path only: the hardware reciprocal (1 ulp)
+                asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv_one_m) : "f"(one_m));
+                float P = 0.0f;
+  #pragma unroll
+                for (int ch = 0; ch < 3; ++ch) {
+                  const float q = (fin[ch] - o[ch]) * inv_one_m;
+                  P = fmaf(go[ch], fmaf(y[ch], T, -q), P);
+                }
+                const float dg = P * al * G;
+                const float inv_det = L.inv_det[i];
+                const float tmpx = fmaf(x, cv.w, -(yy * cv.z)) * inv_det;
+                const float tmpy = fmaf(-x, cv.y, yy * cv.x) * inv_det;
+                const float dx = dg * tmpx, dy = dg * tmpy;
+                sc[0] = dx;
+                sc[1] = dy;
+                sc[2] = 0.5f * (dx * tmpx);
+                sc[3] = 0.5f * (dx * tmpy);
+                sc[4] = 0.5f * (dy * tmpy);
+                sc[5] = P * G;
+                T = T * one_m;
               }
-#pragma unroll
-              for (int ch = 0; ch < 3; ++ch)
-                w[ch] = RGB ? coeff * go[ch] : coeff * (y[ch] * (1.0f - y[ch])) * go[ch];
-              const float one_m = fmaf(-al, G, 1.0f);
-              float inv_one_m;  // gradient path only: the hardware reciprocal (1 ulp)
-              asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv_one_m) : "f"(one_m));
-              float P = 0.0f;
-#pragma unroll
-              for (int ch = 0; ch < 3; ++ch) {
-                const float q = (fin[ch] - o[ch]) * inv_one_m;
-                P = fmaf(go[ch], fmaf(y[ch], T, -q), P);
-              }
-              const float dg = P * al * G;
-              const float inv_det = L.inv_det[i];
-              const float tmpx = fmaf(x, cv.w, -(yy * cv.z)) * inv_det;
-              const float tmpy = fmaf(-x, cv.y, yy * cv.x) * inv_det;
-              const float dx = dg * tmpx, dy = dg * tmpy;
-              sc[0] = dx;
-              sc[1] = dy;
-              sc[2] = 0.5f * (dx * tmpx);
-              sc[3] = 0.5f * (dx * tmpy);
-              sc[4] = 0.5f * (dy * tmpy);
-              sc[5] = P * G;
-              T = T * one_m;
             }
           }
         }
-      }
-      if (__ballot_sync(kFull, contrib)) {
-        const float r = warp_sum6(sc, lane);
-        if ((lane & 3) == 0 && (lane >> 2) < 6 && r != 0.0f)
-          atomicAdd(&s_grad[i * NV + (lane >> 2)], r);
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch) Ws[(3 * nslot + ch) * kWStride + lane] = w[ch];
-        if (lane == 0) {
-          slots[nslot] = i;
-          s_touched[i] = 1;
+        if (__ballot_sync(kFull, contrib)) {
+          const float r = warp_sum6(sc, lane);
+          if ((lane & 3) == 0 && (lane >> 2) < 6 && r != 0.0f)
+            atomicAdd(&s_grad[i * NV + (lane >> 2)], r);
+  #pragma unroll
+          for (int ch = 0; ch < 3; ++ch) Ws[(3 * nslot + ch) * kWStride + lane] = w[ch];
+          if (lane == 0) {
+            slots[nslot] = i;
+            s_touched[i] = 1;
+          }
+          if (++nslot == kSlots) {
+            __syncwarp();
+            flush_sh_group<C>(Ws, Ys, slots, nslot, s_grad, lane);
+            __syncwarp();
+            nslot = 0;
+          }
         }
-        if (++nslot == kSlots) {
-          __syncwarp();
-          flush_sh_group<C>(Ws, Ys, slots, nslot, s_grad, lane);
-          __syncwarp();
-          nslot = 0;
-        }
       }
+      if (nslot > 0) {
+        __syncwarp();
+        flush_sh_group<C>(Ws, Ys, slots, nslot, s_grad, lane);
+        __syncwarp();
+      }
+      if (!done && T < thr) done = true;
+      __syncthreads();
+      fold_batch_grads<C>(a, ctx, L, s_grad, s_touched, nk, t, nthr);
     }
-    if (nslot > 0) {
-      __syncwarp();
-      flush_sh_group<C>(Ws, Ys, slots, nslot, s_grad, lane);
-      __syncwarp();
-    }
-    if (!done && T < thr) done = true;
-    __syncthreads();
-    fold_batch_grads<C>(a, ctx, L, s_grad, s_touched, nk, t, nthr);
+    return true;
+  };
+  if constexpr (PERSIST) {
+    for (int64_t work = claim_work<true>(a, &s_work, true); work >= 0;
+         work = claim_work<true>(a, &s_work, false))
+      if (!run_tile(work)) return;
+  } else {
+    run_tile(blockIdx.x);
   }
 }
 
@@ -1160,7 +1209,7 @@ __device__ __forceinline__ float4 warp_block2(float px, float py0, float py1) {
   return make_float4(x0, x1, y0, y1);
 }
 
-template <int C, int MAXT, bool BATCHED, bool RGB = false>
+template <int C, int MAXT, bool BATCHED, bool RGB = false, bool PERSIST = false>
 __global__ void __launch_bounds__(MAXT, MAXT <= 128 ? 4 : 512 / MAXT)
     raster_backward2_kernel(const RasterArgs a) {
   constexpr int CC = Sh<C>::CC, CCP = Sh<C>::CCP, GSH = Sh<C>::GSH;
@@ -1168,6 +1217,7 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 128 ? 4 : 512 / MAXT)
   extern __shared__ float4 smem4[];
   __shared__ int s_wcount[32];
   __shared__ uint64_t s_bar;  // bulk-copy barrier of the SH rows
+  __shared__ int s_work;
   float *smem = reinterpret_cast<float *>(smem4);
   const int B = a.batch;
   const int nthr = blockDim.x, nwarps = nthr >> 5;
@@ -1178,225 +1228,241 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 128 ? 4 : 512 / MAXT)
   int *s_touched = s_slots + nwarps * 8;                                       // [B]
   int *wl = s_touched + B + (threadIdx.x >> 5) * B;                            // [nwarps][B]
 
-  const ViewCtx ctx = make_ctx<BATCHED>(a);
-  if (ctx.gtile < 0) return;  // CTA-uniform: not a tile of the grid
-  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  int gx, gy0;
-  pixel_of2(ctx, t, gx, gy0);
-  const int gy1 = gy0 + 4;
-  const bool in0 = gx < ctx.width && gy0 < ctx.height;
-  const bool in1 = gx < ctx.width && gy1 < ctx.height;
-  const int s0 = a.start[ctx.gtile];
-  const int n = tile_list_length(a, ctx.gtile, s0);
-  if (n <= 0) return;
-  const float px = fmaf((float)gx, ctx.psx, ctx.topleft[0]);
-  const float py0 = fmaf((float)gy0, ctx.psy, ctx.topleft[1]);
-  const float py1 = fmaf((float)gy1, ctx.psy, ctx.topleft[1]);
-  P2Stage S;
-  S.wh = s_stage + warp * kP2StageWords;
-  S.wl = S.wh + 16 * kP2Cols;
-  S.yh = S.wl + 16 * kP2Cols;
-  S.yl = S.yh + 16 * kP2Cols;
-  int *slots = s_slots + warp * 8;
-  float2 Y2a[Sh<C>::NY2], Y2b[Sh<C>::NY2];
-  {
-    float Ya[CC], Yb[CC];
-    if constexpr (RGB) {
-      Ya[0] = 1.0f;
-      Yb[0] = 1.0f;
-    } else {
-      sh_basis<C>(ctx.c2w, px, py0, Ya);
-      sh_basis<C>(ctx.c2w, px, py1, Yb);
+  if (PERSIST && threadIdx.x == 0) mbar_init(&s_bar);  // once per CTA, before any tile's first wait
+  // bulk-copy phases completed by this CTA: the barrier's parity across the
+  // tiles of a persistent grid (one tile per CTA: the batch index's parity)
+  uint32_t nphase = 0;
+  // one tile; false when the CTA must stop (a bulk-copy wait gave up)
+  auto run_tile = [&](int64_t work) -> bool {
+    const ViewCtx ctx = make_ctx<BATCHED>(a, work);
+    if (ctx.gtile < 0) return true;  // CTA-uniform: not a tile of the grid
+    if (!PERSIST && threadIdx.x == 0 && sh_bulk_ok<C>(ctx.sh, ctx.sh_stride))
+      mbar_init(&s_bar);  // ordered before use by the batch loop's first barrier
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    int gx, gy0;
+    pixel_of2(ctx, t, gx, gy0);
+    const int gy1 = gy0 + 4;
+    const bool in0 = gx < ctx.width && gy0 < ctx.height;
+    const bool in1 = gx < ctx.width && gy1 < ctx.height;
+    const int s0 = a.start[ctx.gtile];
+    const int n = tile_list_length(a, ctx.gtile, s0);
+    if (n <= 0) return true;
+    const float px = fmaf((float)gx, ctx.psx, ctx.topleft[0]);
+    const float py0 = fmaf((float)gy0, ctx.psy, ctx.topleft[1]);
+    const float py1 = fmaf((float)gy1, ctx.psy, ctx.topleft[1]);
+    P2Stage S;
+    S.wh = s_stage + warp * kP2StageWords;
+    S.wl = S.wh + 16 * kP2Cols;
+    S.yh = S.wl + 16 * kP2Cols;
+    S.yl = S.yh + 16 * kP2Cols;
+    int *slots = s_slots + warp * 8;
+    float2 Y2a[Sh<C>::NY2], Y2b[Sh<C>::NY2];
+    {
+      float Ya[CC], Yb[CC];
+      if constexpr (RGB) {
+        Ya[0] = 1.0f;
+        Yb[0] = 1.0f;
+      } else {
+        sh_basis<C>(ctx.c2w, px, py0, Ya);
+        sh_basis<C>(ctx.c2w, px, py1, Yb);
+      }
+      pack_basis<C>(Ya, Y2a);
+      pack_basis<C>(Yb, Y2b);
+  #pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        uint32_t hi = 0u, lo = 0u;
+        if (k < CC) split_half2(Ya[k < CC ? k : 0], Yb[k < CC ? k : 0], hi, lo);
+        S.yh[p2_idx(k, lane)] = hi;
+        S.yl[p2_idx(k, lane)] = lo;
+        S.wh[p2_idx(k, lane)] = 0u;  // rows never staged stay finite
+        S.wl[p2_idx(k, lane)] = 0u;
+      }
     }
-    pack_basis<C>(Ya, Y2a);
-    pack_basis<C>(Yb, Y2b);
-#pragma unroll
-    for (int k = 0; k < 16; ++k) {
-      uint32_t hi = 0u, lo = 0u;
-      if (k < CC) split_half2(Ya[k < CC ? k : 0], Yb[k < CC ? k : 0], hi, lo);
-      S.yh[p2_idx(k, lane)] = hi;
-      S.yl[p2_idx(k, lane)] = lo;
-      S.wh[p2_idx(k, lane)] = 0u;  // rows never staged stay finite
-      S.wl[p2_idx(k, lane)] = 0u;
+    // per-pixel state as (pixel A, pixel B) pairs
+    float2 fin2[3] = {f2(0.0f, 0.0f), f2(0.0f, 0.0f), f2(0.0f, 0.0f)};
+    float2 go2[3] = {f2(0.0f, 0.0f), f2(0.0f, 0.0f), f2(0.0f, 0.0f)};
+    if (in0) {
+      const int64_t pix = 3 * ((int64_t)gy0 * ctx.width + gx);
+  #pragma unroll
+      for (int ch = 0; ch < 3; ++ch) {
+        fin2[ch].x = ctx.final_img[pix + ch];
+        go2[ch].x = ctx.grad_out[pix + ch];
+      }
     }
-  }
-  // per-pixel state as (pixel A, pixel B) pairs
-  float2 fin2[3] = {f2(0.0f, 0.0f), f2(0.0f, 0.0f), f2(0.0f, 0.0f)};
-  float2 go2[3] = {f2(0.0f, 0.0f), f2(0.0f, 0.0f), f2(0.0f, 0.0f)};
-  if (in0) {
-    const int64_t pix = 3 * ((int64_t)gy0 * ctx.width + gx);
-#pragma unroll
-    for (int ch = 0; ch < 3; ++ch) {
-      fin2[ch].x = ctx.final_img[pix + ch];
-      go2[ch].x = ctx.grad_out[pix + ch];
+    if (in1) {
+      const int64_t pix = 3 * ((int64_t)gy1 * ctx.width + gx);
+  #pragma unroll
+      for (int ch = 0; ch < 3; ++ch) {
+        fin2[ch].y = ctx.final_img[pix + ch];
+        go2[ch].y = ctx.grad_out[pix + ch];
+      }
     }
-  }
-  if (in1) {
-    const int64_t pix = 3 * ((int64_t)gy1 * ctx.width + gx);
-#pragma unroll
-    for (int ch = 0; ch < 3; ++ch) {
-      fin2[ch].y = ctx.final_img[pix + ch];
-      go2[ch].y = ctx.grad_out[pix + ch];
-    }
-  }
-  float2 o[3] = {f2(0.0f, 0.0f), f2(0.0f, 0.0f), f2(0.0f, 0.0f)};
-  float2 T2 = f2(1.0f, 1.0f);
-  const float thr = a.T_thresh;
-  bool done0 = !in0, done1 = !in1;
-  float tx0, tx1, ty0, ty1;
-  tile_bounds(ctx, tx0, tx1, ty0, ty1);
-  const float4 blk = warp_block2(px, py0, py1);
-  if (t == 0 && sh_bulk_ok<C>(ctx.sh, ctx.sh_stride))
-    mbar_init(&s_bar);  // ordered before use by the loop's first barrier
+    float2 o[3] = {f2(0.0f, 0.0f), f2(0.0f, 0.0f), f2(0.0f, 0.0f)};
+    float2 T2 = f2(1.0f, 1.0f);
+    const float thr = a.T_thresh;
+    bool done0 = !in0, done1 = !in1;
+    float tx0, tx1, ty0, ty1;
+    tile_bounds(ctx, tx0, tx1, ty0, ty1);
+    const float4 blk = warp_block2(px, py0, py1);
 
-  for (int base = 0; base < n; base += B) {
-    if (__syncthreads_and(done0 && done1)) break;
-    const int nb = min(B, n - base);
-    for (int f = t; f < nb * NV; f += nthr) s_grad[f] = 0.0f;
-    for (int j = t; j < nb; j += nthr) s_touched[j] = 0;
-    const int nk = load_batch<C, true>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1,
-                                       s_wcount, &s_bar, (uint32_t)(base / B) & 1u);
-    if (nk < 0) return;  // flagged in g_raster_flags
-    const int nw = __all_sync(kFull, done0 && done1) ? 0 : warp_list(L, nk, blk, wl, lane);
+    for (int base = 0; base < n; base += B) {
+      if (__syncthreads_and(done0 && done1)) break;
+      const int nb = min(B, n - base);
+      for (int f = t; f < nb * NV; f += nthr) s_grad[f] = 0.0f;
+      for (int j = t; j < nb; j += nthr) s_touched[j] = 0;
+      const int nk = load_batch<C, true>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1,
+                                         s_wcount, &s_bar, PERSIST ? (nphase & 1u) : ((uint32_t)(base / B) & 1u));
+      if (nk < 0) return false;  // flagged in g_raster_flags
+      if (PERSIST && sh_bulk_ok<C>(ctx.sh, ctx.sh_stride)) ++nphase;
+      const int nw = __all_sync(kFull, done0 && done1) ? 0 : warp_list(L, nk, blk, wl, lane);
 
-    int nslot = 0;  // warp-uniform: Gaussians staged in this warp's weight matrix
-    for (int j = 0; j < nw; ++j) {
-      const int i = wl[j];
-      if (__all_sync(kFull, done0 && done1)) break;
-      // a pixel stops before the Gaussian once its transmittance is below the
-      // threshold (the reference's per-Gaussian test)
+      int nslot = 0;  // warp-uniform: Gaussians staged in this warp's weight matrix
+      for (int j = 0; j < nw; ++j) {
+        const int i = wl[j];
+        if (__all_sync(kFull, done0 && done1)) break;
+        // a pixel stops before the Gaussian once its transmittance is below the
+        // threshold (the reference's per-Gaussian test)
+        if (!done0 && T2.x < thr) done0 = true;
+        if (!done1 && T2.y < thr) done1 = true;
+        bool c0 = false, c1 = false;
+        float G0 = 0.0f, G1 = 0.0f, tx_0 = 0.0f, ty_0 = 0.0f, tx_1 = 0.0f, ty_1 = 0.0f;
+        const float al = L.alpha[i];
+        const float4 cv = L.cov[i];
+        const float2 m = L.mean[i];
+        if (!(done0 && done1)) {
+          // both pixels' decision paths side by side, without branches: the
+          // radial of gs/src/include/kernels.h:172-187 (one det per Gaussian,
+          // IEEE division), then the exact exponential where it can decide
+          const float2 h = L.box[i];
+          const float x = px - m.x, y0 = py0 - m.y, y1 = py1 - m.y;
+          const float det = fmaf(cv.x, cv.w, -(cv.y * cv.z));
+          tx_0 = fmaf(x, cv.w, -(y0 * cv.z));
+          ty_0 = fmaf(-x, cv.y, y0 * cv.x);
+          tx_1 = fmaf(x, cv.w, -(y1 * cv.z));
+          ty_1 = fmaf(-x, cv.y, y1 * cv.x);
+          float r0 = fmaf(tx_0, x, ty_0 * y0) / det;
+          float r1 = fmaf(tx_1, x, ty_1 * y1) / det;
+          if (r0 < 0.0f) r0 = 1000.0f;
+          if (r1 < 0.0f) r1 = 1000.0f;
+          const bool xin = !(fabsf(x) > h.x);
+          const bool live0 = !done0 && xin && !(fabsf(y0) > h.y) && !surely_skipped(r0, al);
+          const bool live1 = !done1 && xin && !(fabsf(y1) > h.y) && !surely_skipped(r1, al);
+          // a live radial is NaN or in [0, 12]: -r/2 in [-6, 0] (NaN stays NaN)
+          float e0 = gsx_expf_neg(fmaxf(-0.5f * r0, -86.0f));
+          float e1 = gsx_expf_neg(fmaxf(-0.5f * r1, -86.0f));
+          if (r0 != r0) e0 = r0;
+          if (r1 != r1) e1 = r1;
+          c0 = live0 && !(al * e0 < kMinRenderAlpha);
+          c1 = live1 && !(al * e1 < kMinRenderAlpha);
+          G0 = c0 ? e0 : 0.0f;
+          G1 = c1 ? e1 : 0.0f;
+        }
+        float sc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        float2 w[3] = {f2(0.0f, 0.0f), f2(0.0f, 0.0f), f2(0.0f, 0.0f)};
+        if (c0 || c1) {
+          // both pixels at once; a pixel that does not take this Gaussian has
+          // G = 0, so its colour sums and weights are unchanged / zero (its
+          // other terms are finite whenever the Gaussian's record is)
+          const float2 Gp = f2(G0, G1);
+          const float2 al2 = f2(al, al);
+          float2 coeff = __fmul2_rn(__fmul2_rn(al2, T2), Gp);
+          if (isnan(coeff.x)) coeff.x = 0.0f;
+          if (isnan(coeff.y)) coeff.y = 0.0f;
+          const float *s = L.sh + i * GSH;
+          float2 yv[3];
+  #pragma unroll
+          for (int ch = 0; ch < 3; ++ch) {
+            if constexpr (RGB) {
+              const float v = fmaxf(s[ch * CCP], 0.0f);
+              yv[ch] = f2(v, v);
+            } else {
+              yv[ch] = f2(fmaxf(fast_sigmoid(sh_logit<C>(s + ch * CCP, Y2a)), 0.0f),  // NaN -> 0
+                          fmaxf(fast_sigmoid(sh_logit<C>(s + ch * CCP, Y2b)), 0.0f));
+            }
+            o[ch] = __ffma2_rn(coeff, yv[ch], o[ch]);
+          }
+  #pragma unroll
+          for (int ch = 0; ch < 3; ++ch) {
+            if constexpr (RGB) {
+              w[ch] = __fmul2_rn(coeff, go2[ch]);
+            } else {
+              // y (1 - y), with 1 - y as fma(y, -1, 1)
+              const float2 yy = __fmul2_rn(yv[ch], __ffma2_rn(yv[ch], f2(-1.0f, -1.0f), f2(1.0f, 1.0f)));
+              w[ch] = __fmul2_rn(__fmul2_rn(coeff, yy), go2[ch]);
+            }
+          }
+          const float2 one_m = __ffma2_rn(f2(-al, -al), Gp, f2(1.0f, 1.0f));
+          float inv0, inv1;  // gradient path only: the hardware reciprocal (1 ulp)
+          asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv0) : "f"(one_m.x));
+          asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv1) : "f"(one_m.y));
+          const float2 inv_one_m = f2(inv0, inv1);
+          float2 P = f2(0.0f, 0.0f);
+  #pragma unroll
+          for (int ch = 0; ch < 3; ++ch) {
+            // -q = (out - final) / (1 - aG): o - fin as fma(fin, -1, o), exact
+            const float2 nq = __fmul2_rn(__ffma2_rn(fin2[ch], f2(-1.0f, -1.0f), o[ch]), inv_one_m);
+            P = __ffma2_rn(go2[ch], __ffma2_rn(yv[ch], T2, nq), P);
+          }
+          const float2 dg = __fmul2_rn(__fmul2_rn(P, al2), Gp);
+          const float inv_det = L.inv_det[i];
+          const float2 idet = f2(inv_det, inv_det);
+          const float2 tmpx = __fmul2_rn(f2(tx_0, tx_1), idet);
+          const float2 tmpy = __fmul2_rn(f2(ty_0, ty_1), idet);
+          const float2 dx = __fmul2_rn(dg, tmpx), dy = __fmul2_rn(dg, tmpy);
+          const float2 s2 = __fmul2_rn(f2(0.5f, 0.5f), __fmul2_rn(dx, tmpx));
+          const float2 s3 = __fmul2_rn(f2(0.5f, 0.5f), __fmul2_rn(dx, tmpy));
+          const float2 s4 = __fmul2_rn(f2(0.5f, 0.5f), __fmul2_rn(dy, tmpy));
+          const float2 s5 = __fmul2_rn(P, Gp);
+          sc[0] = dx.x + dx.y;
+          sc[1] = dy.x + dy.y;
+          sc[2] = s2.x + s2.y;
+          sc[3] = s3.x + s3.y;
+          sc[4] = s4.x + s4.y;
+          sc[5] = s5.x + s5.y;
+          if (c0) T2.x = T2.x * one_m.x;
+          if (c1) T2.y = T2.y * one_m.y;
+        }
+        if (__ballot_sync(kFull, c0 || c1)) {
+          const float r = warp_sum6(sc, lane);
+          if ((lane & 3) == 0 && (lane >> 2) < 6 && r != 0.0f)
+            atomicAdd(&s_grad[i * NV + (lane >> 2)], r);
+  #pragma unroll
+          for (int ch = 0; ch < 3; ++ch) {
+            uint32_t hi, lo;
+            split_half2(w[ch].x, w[ch].y, hi, lo);
+            S.wh[p2_idx(3 * nslot + ch, lane)] = hi;
+            S.wl[p2_idx(3 * nslot + ch, lane)] = lo;
+          }
+          if (lane == 0) {
+            slots[nslot] = i;
+            s_touched[i] = 1;
+          }
+          if (++nslot == kSlots) {
+            __syncwarp();
+            flush_sh_group2<C>(S, slots, nslot, s_grad, lane);
+            __syncwarp();
+            nslot = 0;
+          }
+        }
+      }
+      if (nslot > 0) {
+        __syncwarp();
+        flush_sh_group2<C>(S, slots, nslot, s_grad, lane);
+        __syncwarp();
+      }
       if (!done0 && T2.x < thr) done0 = true;
       if (!done1 && T2.y < thr) done1 = true;
-      bool c0 = false, c1 = false;
-      float G0 = 0.0f, G1 = 0.0f, tx_0 = 0.0f, ty_0 = 0.0f, tx_1 = 0.0f, ty_1 = 0.0f;
-      const float al = L.alpha[i];
-      const float4 cv = L.cov[i];
-      const float2 m = L.mean[i];
-      if (!(done0 && done1)) {
-        // both pixels' decision paths side by side, without branches: the
-        // radial of gs/src/include/kernels.h:172-187 (one det per Gaussian,
-        // IEEE division), then the exact exponential where it can decide
-        const float2 h = L.box[i];
-        const float x = px - m.x, y0 = py0 - m.y, y1 = py1 - m.y;
-        const float det = fmaf(cv.x, cv.w, -(cv.y * cv.z));
-        tx_0 = fmaf(x, cv.w, -(y0 * cv.z));
-        ty_0 = fmaf(-x, cv.y, y0 * cv.x);
-        tx_1 = fmaf(x, cv.w, -(y1 * cv.z));
-        ty_1 = fmaf(-x, cv.y, y1 * cv.x);
-        float r0 = fmaf(tx_0, x, ty_0 * y0) / det;
-        float r1 = fmaf(tx_1, x, ty_1 * y1) / det;
-        if (r0 < 0.0f) r0 = 1000.0f;
-        if (r1 < 0.0f) r1 = 1000.0f;
-        const bool xin = !(fabsf(x) > h.x);
-        const bool live0 = !done0 && xin && !(fabsf(y0) > h.y) && !surely_skipped(r0, al);
-        const bool live1 = !done1 && xin && !(fabsf(y1) > h.y) && !surely_skipped(r1, al);
-        // a live radial is NaN or in [0, 12]: -r/2 in [-6, 0] (NaN stays NaN)
-        float e0 = gsx_expf_neg(fmaxf(-0.5f * r0, -86.0f));
-        float e1 = gsx_expf_neg(fmaxf(-0.5f * r1, -86.0f));
-        if (r0 != r0) e0 = r0;
-        if (r1 != r1) e1 = r1;
-        c0 = live0 && !(al * e0 < kMinRenderAlpha);
-        c1 = live1 && !(al * e1 < kMinRenderAlpha);
-        G0 = c0 ? e0 : 0.0f;
-        G1 = c1 ? e1 : 0.0f;
-      }
-      float sc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-      float2 w[3] = {f2(0.0f, 0.0f), f2(0.0f, 0.0f), f2(0.0f, 0.0f)};
-      if (c0 || c1) {
-        // both pixels at once; a pixel that does not take this Gaussian has
-        // G = 0, so its colour sums and weights are unchanged / zero (its
-        // other terms are finite whenever the Gaussian's record is)
-        const float2 Gp = f2(G0, G1);
-        const float2 al2 = f2(al, al);
-        float2 coeff = __fmul2_rn(__fmul2_rn(al2, T2), Gp);
-        if (isnan(coeff.x)) coeff.x = 0.0f;
-        if (isnan(coeff.y)) coeff.y = 0.0f;
-        const float *s = L.sh + i * GSH;
-        float2 yv[3];
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch) {
-          if constexpr (RGB) {
-            const float v = fmaxf(s[ch * CCP], 0.0f);
-            yv[ch] = f2(v, v);
-          } else {
-            yv[ch] = f2(fmaxf(fast_sigmoid(sh_logit<C>(s + ch * CCP, Y2a)), 0.0f),  // NaN -> 0
-                        fmaxf(fast_sigmoid(sh_logit<C>(s + ch * CCP, Y2b)), 0.0f));
-          }
-          o[ch] = __ffma2_rn(coeff, yv[ch], o[ch]);
-        }
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch) {
-          if constexpr (RGB) {
-            w[ch] = __fmul2_rn(coeff, go2[ch]);
-          } else {
-            // y (1 - y), with 1 - y as fma(y, -1, 1)
-            const float2 yy = __fmul2_rn(yv[ch], __ffma2_rn(yv[ch], f2(-1.0f, -1.0f), f2(1.0f, 1.0f)));
-            w[ch] = __fmul2_rn(__fmul2_rn(coeff, yy), go2[ch]);
-          }
-        }
-        const float2 one_m = __ffma2_rn(f2(-al, -al), Gp, f2(1.0f, 1.0f));
-        float inv0, inv1;  // gradient path only: the hardware reciprocal (1 ulp)
-        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv0) : "f"(one_m.x));
-        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv1) : "f"(one_m.y));
-        const float2 inv_one_m = f2(inv0, inv1);
-        float2 P = f2(0.0f, 0.0f);
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch) {
-          // -q = (out - final) / (1 - aG): o - fin as fma(fin, -1, o), exact
-          const float2 nq = __fmul2_rn(__ffma2_rn(fin2[ch], f2(-1.0f, -1.0f), o[ch]), inv_one_m);
-          P = __ffma2_rn(go2[ch], __ffma2_rn(yv[ch], T2, nq), P);
-        }
-        const float2 dg = __fmul2_rn(__fmul2_rn(P, al2), Gp);
-        const float inv_det = L.inv_det[i];
-        const float2 idet = f2(inv_det, inv_det);
-        const float2 tmpx = __fmul2_rn(f2(tx_0, tx_1), idet);
-        const float2 tmpy = __fmul2_rn(f2(ty_0, ty_1), idet);
-        const float2 dx = __fmul2_rn(dg, tmpx), dy = __fmul2_rn(dg, tmpy);
-        const float2 s2 = __fmul2_rn(f2(0.5f, 0.5f), __fmul2_rn(dx, tmpx));
-        const float2 s3 = __fmul2_rn(f2(0.5f, 0.5f), __fmul2_rn(dx, tmpy));
-        const float2 s4 = __fmul2_rn(f2(0.5f, 0.5f), __fmul2_rn(dy, tmpy));
-        const float2 s5 = __fmul2_rn(P, Gp);
-        sc[0] = dx.x + dx.y;
-        sc[1] = dy.x + dy.y;
-        sc[2] = s2.x + s2.y;
-        sc[3] = s3.x + s3.y;
-        sc[4] = s4.x + s4.y;
-        sc[5] = s5.x + s5.y;
-        if (c0) T2.x = T2.x * one_m.x;
-        if (c1) T2.y = T2.y * one_m.y;
-      }
-      if (__ballot_sync(kFull, c0 || c1)) {
-        const float r = warp_sum6(sc, lane);
-        if ((lane & 3) == 0 && (lane >> 2) < 6 && r != 0.0f)
-          atomicAdd(&s_grad[i * NV + (lane >> 2)], r);
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch) {
-          uint32_t hi, lo;
-          split_half2(w[ch].x, w[ch].y, hi, lo);
-          S.wh[p2_idx(3 * nslot + ch, lane)] = hi;
-          S.wl[p2_idx(3 * nslot + ch, lane)] = lo;
-        }
-        if (lane == 0) {
-          slots[nslot] = i;
-          s_touched[i] = 1;
-        }
-        if (++nslot == kSlots) {
-          __syncwarp();
-          flush_sh_group2<C>(S, slots, nslot, s_grad, lane);
-          __syncwarp();
-          nslot = 0;
-        }
-      }
+      __syncthreads();
+      fold_batch_grads<C>(a, ctx, L, s_grad, s_touched, nk, t, nthr);
     }
-    if (nslot > 0) {
-      __syncwarp();
-      flush_sh_group2<C>(S, slots, nslot, s_grad, lane);
-      __syncwarp();
-    }
-    if (!done0 && T2.x < thr) done0 = true;
-    if (!done1 && T2.y < thr) done1 = true;
-    __syncthreads();
-    fold_batch_grads<C>(a, ctx, L, s_grad, s_touched, nk, t, nthr);
+    return true;
+  };
+  if constexpr (PERSIST) {
+    for (int64_t work = claim_work<true>(a, &s_work, true); work >= 0;
+         work = claim_work<true>(a, &s_work, false))
+      if (!run_tile(work)) return;
+  } else {
+    run_tile(blockIdx.x);
   }
 }
 
@@ -1404,138 +1470,155 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 128 ? 4 : 512 / MAXT)
 // raster_backward2_kernel): the record and SH row loads of an entry serve
 // both pixels, and the two pixels' exact decision paths run side by side
 // without branches.  Same arithmetic per pair as raster_forward_kernel.
-template <int C, int MAXT, bool BATCHED, bool RGB = false>
+template <int C, int MAXT, bool BATCHED, bool RGB = false, bool PERSIST = false>
 __global__ void __launch_bounds__(MAXT, MAXT <= 128 ? 5 : 640 / MAXT)
     raster_forward2_kernel(const RasterArgs a) {
   constexpr int GSH = Sh<C>::GSH, CCP = Sh<C>::CCP;
   extern __shared__ float4 smem4[];
   __shared__ int s_wcount[32];
   __shared__ uint64_t s_bar;  // bulk-copy barrier of the SH rows
+  __shared__ int s_work;
   const int nthr = blockDim.x;
   const int B = a.batch;
   SmemLayout L = carve<C>(reinterpret_cast<float *>(smem4), B);
   int *wl = reinterpret_cast<int *>(L.sh + B * GSH) + (threadIdx.x >> 5) * B;  // [nwarps][B]
 
-  const ViewCtx ctx = make_ctx<BATCHED>(a);
-  if (ctx.gtile < 0) return;  // CTA-uniform: not a tile of the grid
-  const int t = threadIdx.x, lane = t & 31;
-  int gx, gy0;
-  pixel_of2(ctx, t, gx, gy0);
-  const int gy1 = gy0 + 4;
-  const bool in0 = gx < ctx.width && gy0 < ctx.height;
-  const bool in1 = gx < ctx.width && gy1 < ctx.height;
-  const int s0 = a.start[ctx.gtile];
-  const int n = tile_list_length(a, ctx.gtile, s0);
-  if (n <= 0) {
-    if (ctx.write_empty) {
-      if (in0) {
-        float *dst = ctx.out + 3 * ((int64_t)gy0 * ctx.width + gx);
-        dst[0] = dst[1] = dst[2] = 0.0f;
+  if (PERSIST && threadIdx.x == 0) mbar_init(&s_bar);  // once per CTA, before any tile's first wait
+  // bulk-copy phases completed by this CTA: the barrier's parity across the
+  // tiles of a persistent grid (one tile per CTA: the batch index's parity)
+  uint32_t nphase = 0;
+  // one tile; false when the CTA must stop (a bulk-copy wait gave up)
+  auto run_tile = [&](int64_t work) -> bool {
+    const ViewCtx ctx = make_ctx<BATCHED>(a, work);
+    if (ctx.gtile < 0) return true;  // CTA-uniform: not a tile of the grid
+    if (!PERSIST && threadIdx.x == 0 && sh_bulk_ok<C>(ctx.sh, ctx.sh_stride))
+      mbar_init(&s_bar);  // ordered before use by the batch loop's first barrier
+    const int t = threadIdx.x, lane = t & 31;
+    int gx, gy0;
+    pixel_of2(ctx, t, gx, gy0);
+    const int gy1 = gy0 + 4;
+    const bool in0 = gx < ctx.width && gy0 < ctx.height;
+    const bool in1 = gx < ctx.width && gy1 < ctx.height;
+    const int s0 = a.start[ctx.gtile];
+    const int n = tile_list_length(a, ctx.gtile, s0);
+    if (n <= 0) {
+      if (ctx.write_empty) {
+        if (in0) {
+          float *dst = ctx.out + 3 * ((int64_t)gy0 * ctx.width + gx);
+          dst[0] = dst[1] = dst[2] = 0.0f;
+        }
+        if (in1) {
+          float *dst = ctx.out + 3 * ((int64_t)gy1 * ctx.width + gx);
+          dst[0] = dst[1] = dst[2] = 0.0f;
+        }
       }
-      if (in1) {
-        float *dst = ctx.out + 3 * ((int64_t)gy1 * ctx.width + gx);
-        dst[0] = dst[1] = dst[2] = 0.0f;
+      return true;
+    }
+    const float px = fmaf((float)gx, ctx.psx, ctx.topleft[0]);
+    const float py0 = fmaf((float)gy0, ctx.psy, ctx.topleft[1]);
+    const float py1 = fmaf((float)gy1, ctx.psy, ctx.topleft[1]);
+    float2 Y2a[Sh<C>::NY2], Y2b[Sh<C>::NY2];
+    {
+      float Ya[Sh<C>::CC], Yb[Sh<C>::CC];
+      if constexpr (RGB) {
+        Ya[0] = 1.0f;
+        Yb[0] = 1.0f;
+      } else {
+        sh_basis<C>(ctx.c2w, px, py0, Ya);
+        sh_basis<C>(ctx.c2w, px, py1, Yb);
       }
+      pack_basis<C>(Ya, Y2a);
+      pack_basis<C>(Yb, Y2b);
     }
-    return;
-  }
-  const float px = fmaf((float)gx, ctx.psx, ctx.topleft[0]);
-  const float py0 = fmaf((float)gy0, ctx.psy, ctx.topleft[1]);
-  const float py1 = fmaf((float)gy1, ctx.psy, ctx.topleft[1]);
-  float2 Y2a[Sh<C>::NY2], Y2b[Sh<C>::NY2];
-  {
-    float Ya[Sh<C>::CC], Yb[Sh<C>::CC];
-    if constexpr (RGB) {
-      Ya[0] = 1.0f;
-      Yb[0] = 1.0f;
-    } else {
-      sh_basis<C>(ctx.c2w, px, py0, Ya);
-      sh_basis<C>(ctx.c2w, px, py1, Yb);
-    }
-    pack_basis<C>(Ya, Y2a);
-    pack_basis<C>(Yb, Y2b);
-  }
-  float2 o[3] = {f2(0.0f, 0.0f), f2(0.0f, 0.0f), f2(0.0f, 0.0f)};
-  float2 T2 = f2(1.0f, 1.0f);
-  const float thr = a.T_thresh;
-  bool done0 = !in0, done1 = !in1;
-  float tx0, tx1, ty0, ty1;
-  tile_bounds(ctx, tx0, tx1, ty0, ty1);
-  const float4 blk = warp_block2(px, py0, py1);
-  if (t == 0 && sh_bulk_ok<C>(ctx.sh, ctx.sh_stride))
-    mbar_init(&s_bar);  // ordered before use by the loop's first barrier
+    float2 o[3] = {f2(0.0f, 0.0f), f2(0.0f, 0.0f), f2(0.0f, 0.0f)};
+    float2 T2 = f2(1.0f, 1.0f);
+    const float thr = a.T_thresh;
+    bool done0 = !in0, done1 = !in1;
+    float tx0, tx1, ty0, ty1;
+    tile_bounds(ctx, tx0, tx1, ty0, ty1);
+    const float4 blk = warp_block2(px, py0, py1);
 
-  for (int base = 0; base < n; base += B) {
-    if (__syncthreads_and(done0 && done1)) break;
-    const int nb = min(B, n - base);
-    const int nk = load_batch<C, false>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1,
-                                        s_wcount, &s_bar, (uint32_t)(base / B) & 1u);
-    if (nk < 0) return;  // flagged in g_raster_flags
-    const int nw = __all_sync(kFull, done0 && done1) ? 0 : warp_list(L, nk, blk, wl, lane);
-    for (int j = 0; j < nw; ++j) {
+    for (int base = 0; base < n; base += B) {
+      if (__syncthreads_and(done0 && done1)) break;
+      const int nb = min(B, n - base);
+      const int nk = load_batch<C, false>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1,
+                                          s_wcount, &s_bar, PERSIST ? (nphase & 1u) : ((uint32_t)(base / B) & 1u));
+      if (nk < 0) return false;  // flagged in g_raster_flags
+      if (PERSIST && sh_bulk_ok<C>(ctx.sh, ctx.sh_stride)) ++nphase;
+      const int nw = __all_sync(kFull, done0 && done1) ? 0 : warp_list(L, nk, blk, wl, lane);
+      for (int j = 0; j < nw; ++j) {
+        if (!done0 && T2.x < thr) done0 = true;
+        if (!done1 && T2.y < thr) done1 = true;
+        if (__all_sync(kFull, done0 && done1)) break;
+        if (done0 && done1) continue;
+        const int i = wl[j];
+        const float al = L.alpha[i];
+        const float4 cv = L.cov[i];
+        const float2 m = L.mean[i];
+        const float2 h = L.box[i];
+        const float x = px - m.x, y0 = py0 - m.y, y1 = py1 - m.y;
+        const float det = fmaf(cv.x, cv.w, -(cv.y * cv.z));
+        float r0 = fmaf(fmaf(x, cv.w, -(y0 * cv.z)), x, fmaf(-x, cv.y, y0 * cv.x) * y0) / det;
+        float r1 = fmaf(fmaf(x, cv.w, -(y1 * cv.z)), x, fmaf(-x, cv.y, y1 * cv.x) * y1) / det;
+        if (r0 < 0.0f) r0 = 1000.0f;
+        if (r1 < 0.0f) r1 = 1000.0f;
+        const bool xin = !(fabsf(x) > h.x);
+        const bool live0 = !done0 && xin && !(fabsf(y0) > h.y) && !surely_skipped(r0, al);
+        const bool live1 = !done1 && xin && !(fabsf(y1) > h.y) && !surely_skipped(r1, al);
+        float e0 = gsx_expf_neg(fmaxf(-0.5f * r0, -86.0f));
+        float e1 = gsx_expf_neg(fmaxf(-0.5f * r1, -86.0f));
+        if (r0 != r0) e0 = r0;
+        if (r1 != r1) e1 = r1;
+        const bool c0 = live0 && !(al * e0 < kMinRenderAlpha);
+        const bool c1 = live1 && !(al * e1 < kMinRenderAlpha);
+        if (!(c0 || c1)) continue;
+        const float2 Gp = f2(c0 ? e0 : 0.0f, c1 ? e1 : 0.0f);
+        float2 coeff = __fmul2_rn(__fmul2_rn(f2(al, al), T2), Gp);
+        if (isnan(coeff.x)) coeff.x = 0.0f;
+        if (isnan(coeff.y)) coeff.y = 0.0f;
+        const float *s = L.sh + i * GSH;
+  #pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+          float2 y;
+          if constexpr (RGB) {
+            y = f2(s[ch * CCP], s[ch * CCP]);
+          } else {
+            y = f2(fast_sigmoid(sh_logit<C>(s + ch * CCP, Y2a)),
+                   fast_sigmoid(sh_logit<C>(s + ch * CCP, Y2b)));
+          }
+          // coeff is finite, so y * coeff is NaN exactly when y is; fmaxf
+          // returns its non-NaN operand and y >= 0: the reference's
+          // `if isnan(y * coeff) y = 0`
+          y = f2(fmaxf(y.x, 0.0f), fmaxf(y.y, 0.0f));
+          o[ch] = __ffma2_rn(coeff, y, o[ch]);
+        }
+        const float2 one_m = __ffma2_rn(f2(-al, -al), Gp, f2(1.0f, 1.0f));
+        if (c0) T2.x = T2.x * one_m.x;
+        if (c1) T2.y = T2.y * one_m.y;
+      }
       if (!done0 && T2.x < thr) done0 = true;
       if (!done1 && T2.y < thr) done1 = true;
-      if (__all_sync(kFull, done0 && done1)) break;
-      if (done0 && done1) continue;
-      const int i = wl[j];
-      const float al = L.alpha[i];
-      const float4 cv = L.cov[i];
-      const float2 m = L.mean[i];
-      const float2 h = L.box[i];
-      const float x = px - m.x, y0 = py0 - m.y, y1 = py1 - m.y;
-      const float det = fmaf(cv.x, cv.w, -(cv.y * cv.z));
-      float r0 = fmaf(fmaf(x, cv.w, -(y0 * cv.z)), x, fmaf(-x, cv.y, y0 * cv.x) * y0) / det;
-      float r1 = fmaf(fmaf(x, cv.w, -(y1 * cv.z)), x, fmaf(-x, cv.y, y1 * cv.x) * y1) / det;
-      if (r0 < 0.0f) r0 = 1000.0f;
-      if (r1 < 0.0f) r1 = 1000.0f;
-      const bool xin = !(fabsf(x) > h.x);
-      const bool live0 = !done0 && xin && !(fabsf(y0) > h.y) && !surely_skipped(r0, al);
-      const bool live1 = !done1 && xin && !(fabsf(y1) > h.y) && !surely_skipped(r1, al);
-      float e0 = gsx_expf_neg(fmaxf(-0.5f * r0, -86.0f));
-      float e1 = gsx_expf_neg(fmaxf(-0.5f * r1, -86.0f));
-      if (r0 != r0) e0 = r0;
-      if (r1 != r1) e1 = r1;
-      const bool c0 = live0 && !(al * e0 < kMinRenderAlpha);
-      const bool c1 = live1 && !(al * e1 < kMinRenderAlpha);
-      if (!(c0 || c1)) continue;
-      const float2 Gp = f2(c0 ? e0 : 0.0f, c1 ? e1 : 0.0f);
-      float2 coeff = __fmul2_rn(__fmul2_rn(f2(al, al), T2), Gp);
-      if (isnan(coeff.x)) coeff.x = 0.0f;
-      if (isnan(coeff.y)) coeff.y = 0.0f;
-      const float *s = L.sh + i * GSH;
-#pragma unroll
-      for (int ch = 0; ch < 3; ++ch) {
-        float2 y;
-        if constexpr (RGB) {
-          y = f2(s[ch * CCP], s[ch * CCP]);
-        } else {
-          y = f2(fast_sigmoid(sh_logit<C>(s + ch * CCP, Y2a)),
-                 fast_sigmoid(sh_logit<C>(s + ch * CCP, Y2b)));
-        }
-        // coeff is finite, so y * coeff is NaN exactly when y is; fmaxf
-        // returns its non-NaN operand and y >= 0: the reference's
-        // `if isnan(y * coeff) y = 0`
-        y = f2(fmaxf(y.x, 0.0f), fmaxf(y.y, 0.0f));
-        o[ch] = __ffma2_rn(coeff, y, o[ch]);
-      }
-      const float2 one_m = __ffma2_rn(f2(-al, -al), Gp, f2(1.0f, 1.0f));
-      if (c0) T2.x = T2.x * one_m.x;
-      if (c1) T2.y = T2.y * one_m.y;
     }
-    if (!done0 && T2.x < thr) done0 = true;
-    if (!done1 && T2.y < thr) done1 = true;
-  }
-  if (in0) {
-    float *dst = ctx.out + 3 * ((int64_t)gy0 * ctx.width + gx);
-    dst[0] = o[0].x;
-    dst[1] = o[1].x;
-    dst[2] = o[2].x;
-  }
-  if (in1) {
-    float *dst = ctx.out + 3 * ((int64_t)gy1 * ctx.width + gx);
-    dst[0] = o[0].y;
-    dst[1] = o[1].y;
-    dst[2] = o[2].y;
+    if (in0) {
+      float *dst = ctx.out + 3 * ((int64_t)gy0 * ctx.width + gx);
+      dst[0] = o[0].x;
+      dst[1] = o[1].x;
+      dst[2] = o[2].x;
+    }
+    if (in1) {
+      float *dst = ctx.out + 3 * ((int64_t)gy1 * ctx.width + gx);
+      dst[0] = o[0].y;
+      dst[1] = o[1].y;
+      dst[2] = o[2].y;
+    }
+    return true;
+  };
+  if constexpr (PERSIST) {
+    for (int64_t work = claim_work<true>(a, &s_work, true); work >= 0;
+         work = claim_work<true>(a, &s_work, false))
+      if (!run_tile(work)) return;
+  } else {
+    run_tile(blockIdx.x);
   }
 }
 
@@ -1568,6 +1651,26 @@ cudaError_t ensure_smem(K kernel, size_t smem, size_t &done) {
   return e;
 }
 
+// Grid of a raster launch over a.n_work = `items` tiles: one CTA per tile,
+// or, with a work counter, as many CTAs as the SMs hold at once (the counter
+// is zeroed first, on the launch's stream).
+template <typename K>
+cudaError_t raster_grid(K kernel, int nthr, size_t smem, int64_t items, RasterArgs &a,
+                        cudaStream_t s, unsigned &grid) {
+  a.n_work = items;
+  grid = (unsigned)items;
+  if (!a.work_counter) return cudaSuccess;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, nthr, smem);
+  if (e == cudaSuccess) e = cudaMemsetAsync(a.work_counter, 0, sizeof(uint32_t), s);
+  if (e != cudaSuccess) return e;
+  const int64_t resident = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
+  grid = (unsigned)(items < resident ? items : resident);
+  return cudaSuccess;
+}
+
 // The two-pixel raster kernels cover tiles made of 8x8 blocks, up to 1024
 // pixels.
 inline bool two_pixel_tiles(const RasterArgs &a) {
@@ -1593,11 +1696,26 @@ int launch_fwd_tt(RasterArgs a, int64_t grid, cudaStream_t s) {
   const int nthr = block_threads(a);
   a.batch = nthr < 128 ? nthr : 128;
   const size_t smem = fwd_smem<C>(a.batch, nthr);
-  static size_t attr_done = 0;
+  static size_t attr_done = 0, attr_done_p = 0;
   cudaError_t e = ensure_smem(raster_forward_kernel<C, MAXT, BATCHED, EXTRAS, RGB>, smem, attr_done);
   if (e != cudaSuccess) return cuda_status(e, "raster_forward smem attribute");
+  unsigned launch_grid = 0;
+  if constexpr (BATCHED) {
+    if (a.work_counter) {  // persistent grid over the batch's tiles
+      auto kp = raster_forward_kernel<C, MAXT, BATCHED, EXTRAS, RGB, true>;
+      e = ensure_smem(kp, smem, attr_done_p);
+      if (e == cudaSuccess) e = raster_grid(kp, nthr, smem, grid, a, s, launch_grid);
+      if (e != cudaSuccess) return cuda_status(e, "raster grid");
+      count_launches(1);
+      kp<<<launch_grid, nthr, smem, s>>>(a);
+      return cuda_status(cudaGetLastError(), "raster_forward_kernel launch");
+    }
+  }
+  a.work_counter = nullptr;
+  e = raster_grid(raster_forward_kernel<C, MAXT, BATCHED, EXTRAS, RGB>, nthr, smem, grid, a, s, launch_grid);
+  if (e != cudaSuccess) return cuda_status(e, "raster grid");
   count_launches(1);
-  raster_forward_kernel<C, MAXT, BATCHED, EXTRAS, RGB><<<(unsigned)grid, nthr, smem, s>>>(a);
+  raster_forward_kernel<C, MAXT, BATCHED, EXTRAS, RGB><<<launch_grid, nthr, smem, s>>>(a);
   return cuda_status(cudaGetLastError(), "raster_forward_kernel launch");
 }
 
@@ -1606,11 +1724,26 @@ int launch_fwd2_tt(RasterArgs a, int64_t grid, cudaStream_t s) {
   const int nthr = a.tile_w * a.tile_h / 2;
   a.batch = nthr < 128 ? nthr : 128;
   const size_t smem = fwd_smem<C>(a.batch, nthr);
-  static size_t attr_done = 0;
+  static size_t attr_done = 0, attr_done_p = 0;
   cudaError_t e = ensure_smem(raster_forward2_kernel<C, MAXT, BATCHED, RGB>, smem, attr_done);
   if (e != cudaSuccess) return cuda_status(e, "raster_forward2 smem attribute");
+  unsigned launch_grid = 0;
+  if constexpr (BATCHED) {
+    if (a.work_counter) {  // persistent grid over the batch's tiles
+      auto kp = raster_forward2_kernel<C, MAXT, BATCHED, RGB, true>;
+      e = ensure_smem(kp, smem, attr_done_p);
+      if (e == cudaSuccess) e = raster_grid(kp, nthr, smem, grid, a, s, launch_grid);
+      if (e != cudaSuccess) return cuda_status(e, "raster grid");
+      count_launches(1);
+      kp<<<launch_grid, nthr, smem, s>>>(a);
+      return cuda_status(cudaGetLastError(), "raster_forward2_kernel launch");
+    }
+  }
+  a.work_counter = nullptr;
+  e = raster_grid(raster_forward2_kernel<C, MAXT, BATCHED, RGB>, nthr, smem, grid, a, s, launch_grid);
+  if (e != cudaSuccess) return cuda_status(e, "raster grid");
   count_launches(1);
-  raster_forward2_kernel<C, MAXT, BATCHED, RGB><<<(unsigned)grid, nthr, smem, s>>>(a);
+  raster_forward2_kernel<C, MAXT, BATCHED, RGB><<<launch_grid, nthr, smem, s>>>(a);
   return cuda_status(cudaGetLastError(), "raster_forward2_kernel launch");
 }
 
@@ -1643,11 +1776,26 @@ int launch_bwd_tt(RasterArgs a, int64_t grid, cudaStream_t s) {
                     : 0;
   a.batch = nthr < 64 ? nthr : 64;
   const size_t smem = bwd_smem<C>(a.batch, nthr);
-  static size_t attr_done = 0;
+  static size_t attr_done = 0, attr_done_p = 0;
   cudaError_t e = ensure_smem(raster_backward_kernel<C, MAXT, BATCHED, RGB>, smem, attr_done);
   if (e != cudaSuccess) return cuda_status(e, "raster_backward smem attribute");
+  unsigned launch_grid = 0;
+  if constexpr (BATCHED) {
+    if (a.work_counter) {  // persistent grid over the batch's tiles
+      auto kp = raster_backward_kernel<C, MAXT, BATCHED, RGB, true>;
+      e = ensure_smem(kp, smem, attr_done_p);
+      if (e == cudaSuccess) e = raster_grid(kp, nthr, smem, grid, a, s, launch_grid);
+      if (e != cudaSuccess) return cuda_status(e, "raster grid");
+      count_launches(1);
+      kp<<<launch_grid, nthr, smem, s>>>(a);
+      return cuda_status(cudaGetLastError(), "raster_backward_kernel launch");
+    }
+  }
+  a.work_counter = nullptr;
+  e = raster_grid(raster_backward_kernel<C, MAXT, BATCHED, RGB>, nthr, smem, grid, a, s, launch_grid);
+  if (e != cudaSuccess) return cuda_status(e, "raster grid");
   count_launches(1);
-  raster_backward_kernel<C, MAXT, BATCHED, RGB><<<(unsigned)grid, nthr, smem, s>>>(a);
+  raster_backward_kernel<C, MAXT, BATCHED, RGB><<<launch_grid, nthr, smem, s>>>(a);
   return cuda_status(cudaGetLastError(), "raster_backward_kernel launch");
 }
 
@@ -1676,11 +1824,26 @@ int launch_bwd2_tt(RasterArgs a, int64_t grid, cudaStream_t s) {
                     : 0;
   a.batch = nthr < GSX_BWD2_BATCH ? nthr : GSX_BWD2_BATCH;
   const size_t smem = bwd2_smem<C>(a.batch, nthr);
-  static size_t attr_done = 0;
+  static size_t attr_done = 0, attr_done_p = 0;
   cudaError_t e = ensure_smem(raster_backward2_kernel<C, MAXT, BATCHED, RGB>, smem, attr_done);
   if (e != cudaSuccess) return cuda_status(e, "raster_backward2 smem attribute");
+  unsigned launch_grid = 0;
+  if constexpr (BATCHED) {
+    if (a.work_counter) {  // persistent grid over the batch's tiles
+      auto kp = raster_backward2_kernel<C, MAXT, BATCHED, RGB, true>;
+      e = ensure_smem(kp, smem, attr_done_p);
+      if (e == cudaSuccess) e = raster_grid(kp, nthr, smem, grid, a, s, launch_grid);
+      if (e != cudaSuccess) return cuda_status(e, "raster grid");
+      count_launches(1);
+      kp<<<launch_grid, nthr, smem, s>>>(a);
+      return cuda_status(cudaGetLastError(), "raster_backward2_kernel launch");
+    }
+  }
+  a.work_counter = nullptr;
+  e = raster_grid(raster_backward2_kernel<C, MAXT, BATCHED, RGB>, nthr, smem, grid, a, s, launch_grid);
+  if (e != cudaSuccess) return cuda_status(e, "raster grid");
   count_launches(1);
-  raster_backward2_kernel<C, MAXT, BATCHED, RGB><<<(unsigned)grid, nthr, smem, s>>>(a);
+  raster_backward2_kernel<C, MAXT, BATCHED, RGB><<<launch_grid, nthr, smem, s>>>(a);
   return cuda_status(cudaGetLastError(), "raster_backward2_kernel launch");
 }
 

@@ -43,7 +43,9 @@ const char *gsx_status_string(int status);
 const char *gsx_last_error(void);
 /* ABI version of this library (increments on any signature change). */
 /* 2: gsx_project_backward / gsx_batch_project_backward take grad_flags;
-   3: gsx_raster_params gains pixels_per_thread */
+   3: gsx_raster_params gains pixels_per_thread, gsx_batch_view's spare
+      int32 becomes pixels_per_thread, the batched raster passes take
+      tile_order and work_counter */
 #define GSX_ABI_VERSION 3
 int gsx_abi_version(void);
 /* Number of kernels this library has launched in this process so far. */
@@ -181,7 +183,8 @@ typedef struct gsx_batch_view {
   float pixel_size_x, pixel_size_y;
   float *out;            /* [height, width, 3] */
   const float *grad_out; /* dL/dout [height, width, 3] (backward) */
-  int32_t write_empty_tiles, reserved;
+  int32_t write_empty_tiles;
+  int32_t pixels_per_thread; /* raster schedule as in gsx_raster_params; the same in every view */
   gsx_camera cam;
 } gsx_batch_view;
 
@@ -210,16 +213,26 @@ int gsx_batch_bin_async(const gsx_batch_view *views_dev, const gsx_batch_view *v
                         const float *depth, int64_t key_capacity, int32_t *gaussian_ids,
                         int32_t *start, int32_t *end, void *workspace, size_t workspace_bytes,
                         void *stream);
+/*
+ * The batched raster passes.  tile_order (i32[total tiles], e.g. from
+ * gsx_tile_order over the batch's start/end; NULL = tile index order) and
+ * work_counter (one u32 of device memory; NULL = one CTA per tile) make the
+ * launch persistent: as many CTAs as the SMs hold at once claim the tiles,
+ * longest lists first, one atomic per tile.  The counter is zeroed on
+ * `stream` before the launch; the two passes may share it when they run on
+ * one stream.  Images and gradients do not depend on either.
+ */
 int gsx_batch_render_forward(const gsx_batch_view *views_dev, const gsx_batch_view *views_host,
                              int32_t n_views, int64_t key_capacity, const float *mean2d,
                              const float *cov2d, const float *alpha, const int32_t *start,
                              const int32_t *end, const int32_t *gaussian_ids, float T_thresh,
-                             void *stream);
+                             const int32_t *tile_order, uint32_t *work_counter, void *stream);
 int gsx_batch_render_backward(const gsx_batch_view *views_dev, const gsx_batch_view *views_host,
                               int32_t n_views, int64_t key_capacity, const float *mean2d,
                               const float *cov2d, const float *alpha, const int32_t *start,
                               const int32_t *end, const int32_t *gaussian_ids, float *g_mean2d,
-                              float *g_cov2d, float *g_alpha, float T_thresh, void *stream);
+                              float *g_cov2d, float *g_alpha, float T_thresh,
+                              const int32_t *tile_order, uint32_t *work_counter, void *stream);
 int gsx_batch_project_backward(const gsx_batch_view *views_dev, const gsx_batch_view *views_host,
                                int32_t n_views, const int32_t *counts, const float *g_mean2d,
                                const float *g_cov2d, const float *g_alpha, int32_t grad_flags,

@@ -115,8 +115,32 @@ def test_autotuner_picks_a_listed_shape():
     scene_t = B.Scene.from_arrays(sc, dev())
     views = [B.ViewSpec(0, c, cam) for c, cam in make_views(2, seed=62)]
     best, times = B.autotune_tile([scene_t], views, reps=1, device=dev())
-    assert best in times and set(times) == {(8, 8), (16, 16), (32, 8)}
+    shapes = {(8, 8), (16, 16), (32, 8)}
+    assert best in times and set(times) == {(w, h, p) for w, h in shapes for p in (0, 1, 2)}
     assert all(t > 0 for t in times.values())
+
+
+def test_batched_schedules_give_the_same_images_and_close_gradients():
+    """Pixels per thread in the batched raster passes: images bit-identical,
+    gradients within the parity tolerance of one another."""
+    sc = S.custom_workload(3000, 64, 64, 3, seed=63).scene
+    scene_t = B.Scene.from_arrays(sc, dev())
+    views = [B.ViewSpec(0, c, cam) for c, cam in make_views(3, seed=64)]
+    runs = []
+    for ppt in (1, 2):
+        bp = B.BatchPipeline(dev(), renderer.RasterSettings(pixels_per_thread=ppt)).plan([scene_t], views)
+        gen = torch.Generator(device="cpu").manual_seed(5)
+        for g in bp.grad_outs:
+            g.copy_(torch.rand(g.shape, generator=gen))
+        bp.step()
+        torch.cuda.synchronize()
+        runs.append(([im.cpu().numpy() for im in bp.images],
+                     [t.cpu().numpy().astype(np.float64) for t in (bp.g_mean, bp.g_qvec, bp.g_log_scale, bp.g_sh,
+                                                                   bp.g_alpha_logit)]))
+    for a, b in zip(runs[0][0], runs[1][0]):
+        np.testing.assert_array_equal(a, b)
+    for a, b in zip(runs[0][1], runs[1][1]):
+        assert np.abs(a - b).max() <= 1e-4 * max(np.abs(b).max(), 1e-3)
 
 
 def test_batch_with_more_than_65536_tiles_matches_per_view():
@@ -137,3 +161,28 @@ def test_batch_with_more_than_65536_tiles_matches_per_view():
     for i, (c2w, cam) in enumerate(views):
         img = renderer.rasterize(*params, c2w, cam, st)
         np.testing.assert_array_equal(bp.images[i].cpu().numpy(), img.cpu().numpy())
+
+
+def test_persistent_raster_matches_one_cta_per_tile():
+    """The persistent raster grids (tiles claimed longest first through a
+    work counter) give the images of one CTA per tile bit for bit and the
+    gradients within the parity tolerance."""
+    sc = S.custom_workload(3000, 64, 64, 3, seed=65).scene
+    scene_t = B.Scene.from_arrays(sc, dev())
+    views = [B.ViewSpec(0, c, cam) for c, cam in make_views(4, seed=66)]
+    runs = []
+    for persistent in (False, True):
+        bp = B.BatchPipeline(dev(), renderer.RasterSettings(), persistent=persistent).plan([scene_t], views)
+        gen = torch.Generator(device="cpu").manual_seed(6)
+        for g in bp.grad_outs:
+            g.copy_(torch.rand(g.shape, generator=gen))
+        bp.step()
+        bp.step()  # the counter is zeroed per launch: a second step claims every tile again
+        torch.cuda.synchronize()
+        runs.append(([im.cpu().numpy() for im in bp.images],
+                     [t.cpu().numpy().astype(np.float64) for t in (bp.g_mean, bp.g_qvec, bp.g_log_scale, bp.g_sh,
+                                                                   bp.g_alpha_logit)]))
+    for a, b in zip(runs[0][0], runs[1][0]):
+        np.testing.assert_array_equal(a, b)
+    for a, b in zip(runs[0][1], runs[1][1]):
+        assert np.abs(a - b).max() <= 1e-4 * max(np.abs(b).max(), 1e-3)
