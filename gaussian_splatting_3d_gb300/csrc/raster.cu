@@ -51,8 +51,6 @@ __device__ uint32_t g_raster_flags = 0;
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-// polls of a bulk-copy barrier before the raster gives up and flags the error
-constexpr uint32_t kBulkWaitLimit = 1u << 20;
 constexpr uint32_t kRasterErrTimeout = 1u;  // bit of g_raster_flags
 
 template <int C>
@@ -374,52 +372,8 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 // ---- bulk-copy (TMA engine) staging of the SH rows -------------------------
 // A batch's SH rows are copied global -> shared with cp.async.bulk, one copy
 // per kept Gaussian (or per channel when the rows are strided), completing on
-// one mbarrier per CTA.  Thread 0 arms the barrier with the batch's byte
-// total; the phase flips once per batch.
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Bounded wait for the phase `parity` of `bar`; false if it did not complete.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
-  for (uint32_t i = 0; i < kBulkWaitLimit; ++i)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
-}
-
-__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes,
-                                              uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
-          "r"(smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
+// one mbarrier per CTA (helpers in gsx_internal.cuh).  Thread 0 arms the
+// barrier with the batch's byte total; the phase flips once per batch.
 
 // Diagnostic of the bounded wait: one CTA polls a barrier phase that cannot
 // complete (two arrivals expected, one made, no copies), gives up after
