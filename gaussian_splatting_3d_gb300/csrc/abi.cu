@@ -681,7 +681,10 @@ int gsx_photometric_loss(const float *out, const float *gt, int32_t height, int3
                          float *partials, void *workspace, size_t workspace_bytes, void *stream) {
   g_err[0] = 0;
   GSX_REQUIRE(height > 0 && width > 0, "image size must be positive");
-  GSX_REQUIRE(win_size >= 1 && win_size <= 31 && (win_size & 1), "win_size must be odd, 1..31");
+  GSX_REQUIRE(win_size >= 1 && win_size <= 31 && (win_size & 1),
+              "win_size must be odd, 1..31 (got %d; kornia centres an even window between "
+              "pixels, which these kernels do not)",
+              win_size);
   GSX_REQUIRE(win_size / 2 < height && win_size / 2 < width,
               "reflected borders need the window radius below the image size");
   GSX_REQUIRE(ssim_mult >= 0.0f && ssim_mult <= 1.0f, "ssim_mult must be in [0, 1]");

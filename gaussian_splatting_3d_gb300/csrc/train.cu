@@ -4,9 +4,11 @@
 //
 // Loss (utils/loss.py:5-24): L = m * SSIM_loss(out, gt) + (1 - m) * base(out,
 // gt), base = L1 or L2 (mean), SSIM_loss = mean(clamp((1 - SSIM) / 2, 0, 1))
-// over channels and pixels, with kornia's published SSIM: an 11x11 (any odd
-// size) normalised Gaussian window of sigma 1.5 applied per channel with
-// reflected borders ("same" size), C1 = 0.01^2, C2 = 0.03^2,
+// over channels and pixels, with the SSIM of the kornia 0.6 series (the one
+// the reference's imports fit: kornia.metrics.ssim / kornia.losses.ssim_loss):
+// an 11x11 (any odd size; even sizes are rejected) normalised Gaussian window
+// of sigma 1.5 applied per channel with reflected borders ("same" size),
+// C1 = 0.01^2, C2 = 0.03^2,
 // SSIM = (2 mu1 mu2 + C1)(2 s12 + C2) / ((mu1^2 + mu2^2 + C1)(s1 + s2 + C2) + eps).
 // The gradient with respect to `out` runs the window filter's adjoint
 // (reflection folded back onto the border pixels), so it is the exact

@@ -2,7 +2,9 @@
 
 * photometric loss: value within 1e-5 relative and dL/dout within 1e-4 *
   max |reference| of torch autograd through the FP64 restatement of the
-  reference's loss (oracle/loss_ref.py), for L1 and L2, windows 11 and 7,
+  reference's loss with the kornia 0.6 series' SSIM (oracle/loss_ref.py;
+  utils/loss.py:15-20 calls kornia.losses.ssim_loss), for L1 and L2, windows
+  11 (the reference's configuration) and 7,
   images with identical regions (the clamp and the L1 kink);
 * FusedAdam: three steps with per-group learning rates equal torch.optim.Adam
   (the reference's optimizer, betas (0.9, 0.99)) within 1e-6 relative.
