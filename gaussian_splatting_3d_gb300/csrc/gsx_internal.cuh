@@ -42,10 +42,10 @@ __device__ __forceinline__ float gsx_expf(float x) {
   return p * __int_as_float((ji + 127) << 23);
 }
 
-// gsx_expf for x in [-86, 0], the range of every raster decision: the same
-// operation sequence without the range branches, and j taken from the bits
-// of the rounding sum t = 1.5 * 2^23 + j (exact for |j| < 2^22) instead of a
-// float -> int conversion, so it returns gsx_expf(x) bit for bit there.
+// gsx_expf for x in (-87, 0]: the same operation sequence without the range
+// branches, and j taken from the bits of the rounding sum t = 1.5 * 2^23 + j
+// (exact for |j| < 2^22) instead of a float -> int conversion, so it returns
+// gsx_expf(x) bit for bit there (j >= -126: the scale 2^j stays normal).
 __device__ __forceinline__ float gsx_expf_neg(float x) {
   float t = fmaf(x, 1.44269502162933349609375f, 12582912.0f);
   float j = t - 12582912.0f;
@@ -61,6 +61,14 @@ __device__ __forceinline__ float gsx_expf_neg(float x) {
   p = fmaf(p, r, 1.0f);
   const int ji = __float_as_int(t) - 0x4B400000;  // t = 12582912 + j
   return p * __int_as_float((ji + 127) << 23);
+}
+
+// gsx_expf for every x <= 0 and NaN (the raster's exponent -radial/2),
+// without branches: equal to gsx_expf there bit for bit (+0 at and below
+// -87, NaN for NaN).
+__device__ __forceinline__ float gsx_expf_nonpos(float x) {
+  const float e = gsx_expf_neg(fmaxf(x, -87.0f));
+  return x > -87.0f ? e : (x != x ? x : 0.0f);
 }
 
 __device__ __forceinline__ float gsx_sigmoidf(float x) {

@@ -633,7 +633,7 @@ __global__ void __launch_bounds__(MAXT) raster_forward_kernel(const RasterArgs a
           const float al = L.alpha[i];
           const float radial = radial_of(L.cov[i], x, y);
           if (surely_skipped(radial, al)) continue;
-          const float G = gsx_expf(-0.5f * radial);
+          const float G = gsx_expf_nonpos(-0.5f * radial);
           float coeff = al * T;
           coeff = coeff * G;
           if (al * G < kMinRenderAlpha) continue;
@@ -910,13 +910,13 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
       if constexpr (RGB) Y[0] = 1.0f;
       else sh_basis<C>(ctx.c2w, px, py, Y);
       pack_basis<C>(Y, Y2);
-  #pragma unroll
+#pragma unroll
       for (int k = 0; k < 16; ++k) Ys[k * kYStride + lane] = k < CC ? Y[k < CC ? k : 0] : 0.0f;
     }
     float fin[3] = {0.0f, 0.0f, 0.0f}, go[3] = {0.0f, 0.0f, 0.0f};
     if (inside) {
       const int64_t pix = 3 * ((int64_t)gy * ctx.width + gx);
-  #pragma unroll
+#pragma unroll
       for (int ch = 0; ch < 3; ++ch) {
         fin[ch] = ctx.final_img[pix + ch];
         go[ch] = ctx.grad_out[pix + ch];
@@ -960,27 +960,27 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
             const bool outside = fabsf(x) > h.x || fabsf(yy) > h.y;
             const float radial = outside ? 0.0f : radial_of(cv, x, yy);
             if (!outside && !surely_skipped(radial, al)) {
-              const float G = gsx_expf(-0.5f * radial);
+              const float G = gsx_expf_nonpos(-0.5f * radial);
               if (!(al * G < kMinRenderAlpha)) {
                 contrib = true;
                 float coeff = al * T * G;
                 if (isnan(coeff)) coeff = 0.0f;
                 const float *s = L.sh + i * GSH;
                 float y[3];
-  #pragma unroll
+#pragma unroll
                 for (int ch = 0; ch < 3; ++ch) {
                   y[ch] = RGB ? fmaxf(s[ch * CCP], 0.0f)
                               : fmaxf(fast_sigmoid(sh_logit<C>(s + ch * CCP, Y2)), 0.0f);  // NaN -> 0
                   o[ch] = fmaf(coeff, y[ch], o[ch]);
                 }
-  #pragma unroll
+#pragma unroll
                 for (int ch = 0; ch < 3; ++ch)
                   w[ch] = RGB ? coeff * go[ch] : coeff * (y[ch] * (1.0f - y[ch])) * go[ch];
                 const float one_m = fmaf(-al, G, 1.0f);
                 float inv_one_m;  // gradient path only: the hardware reciprocal (1 ulp)
                 asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv_one_m) : "f"(one_m));
                 float P = 0.0f;
-  #pragma unroll
+#pragma unroll
                 for (int ch = 0; ch < 3; ++ch) {
                   const float q = (fin[ch] - o[ch]) * inv_one_m;
                   P = fmaf(go[ch], fmaf(y[ch], T, -q), P);
@@ -1005,7 +1005,7 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
           const float r = warp_sum6(sc, lane);
           if ((lane & 3) == 0 && (lane >> 2) < 6 && r != 0.0f)
             atomicAdd(&s_grad[i * NV + (lane >> 2)], r);
-  #pragma unroll
+#pragma unroll
           for (int ch = 0; ch < 3; ++ch) Ws[(3 * nslot + ch) * kWStride + lane] = w[ch];
           if (lane == 0) {
             slots[nslot] = i;
@@ -1222,7 +1222,7 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 128 ? 4 : 512 / MAXT)
       }
       pack_basis<C>(Ya, Y2a);
       pack_basis<C>(Yb, Y2b);
-  #pragma unroll
+#pragma unroll
       for (int k = 0; k < 16; ++k) {
         uint32_t hi = 0u, lo = 0u;
         if (k < CC) split_half2(Ya[k < CC ? k : 0], Yb[k < CC ? k : 0], hi, lo);
@@ -1237,7 +1237,7 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 128 ? 4 : 512 / MAXT)
     float2 go2[3] = {f2(0.0f, 0.0f), f2(0.0f, 0.0f), f2(0.0f, 0.0f)};
     if (in0) {
       const int64_t pix = 3 * ((int64_t)gy0 * ctx.width + gx);
-  #pragma unroll
+#pragma unroll
       for (int ch = 0; ch < 3; ++ch) {
         fin2[ch].x = ctx.final_img[pix + ch];
         go2[ch].x = ctx.grad_out[pix + ch];
@@ -1245,7 +1245,7 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 128 ? 4 : 512 / MAXT)
     }
     if (in1) {
       const int64_t pix = 3 * ((int64_t)gy1 * ctx.width + gx);
-  #pragma unroll
+#pragma unroll
       for (int ch = 0; ch < 3; ++ch) {
         fin2[ch].y = ctx.final_img[pix + ch];
         go2[ch].y = ctx.grad_out[pix + ch];
@@ -1301,12 +1301,9 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 128 ? 4 : 512 / MAXT)
           const bool xin = !(fabsf(x) > h.x);
           const bool live0 = !done0 && xin && !(fabsf(y0) > h.y) && !surely_skipped(r0, al);
           const bool live1 = !done1 && xin && !(fabsf(y1) > h.y) && !surely_skipped(r1, al);
-          // a live radial is NaN or in [0, 12]: -r/2 in [-6, 0] (NaN stays NaN)
-          float e0 = gsx_expf_neg(fmaxf(-0.5f * r0, -86.0f));
-          float e1 = gsx_expf_neg(fmaxf(-0.5f * r1, -86.0f));
-          if (r0 != r0) e0 = r0;
-          if (r1 != r1) e1 = r1;
-          c0 = live0 && !(al * e0 < kMinRenderAlpha);
+          const float e0 = gsx_expf_nonpos(-0.5f * r0);
+          const float e1 = gsx_expf_nonpos(-0.5f * r1);
+              c0 = live0 && !(al * e0 < kMinRenderAlpha);
           c1 = live1 && !(al * e1 < kMinRenderAlpha);
           G0 = c0 ? e0 : 0.0f;
           G1 = c1 ? e1 : 0.0f;
@@ -1324,7 +1321,7 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 128 ? 4 : 512 / MAXT)
           if (isnan(coeff.y)) coeff.y = 0.0f;
           const float *s = L.sh + i * GSH;
           float2 yv[3];
-  #pragma unroll
+#pragma unroll
           for (int ch = 0; ch < 3; ++ch) {
             if constexpr (RGB) {
               const float v = fmaxf(s[ch * CCP], 0.0f);
@@ -1335,7 +1332,7 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 128 ? 4 : 512 / MAXT)
             }
             o[ch] = __ffma2_rn(coeff, yv[ch], o[ch]);
           }
-  #pragma unroll
+#pragma unroll
           for (int ch = 0; ch < 3; ++ch) {
             if constexpr (RGB) {
               w[ch] = __fmul2_rn(coeff, go2[ch]);
@@ -1351,7 +1348,7 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 128 ? 4 : 512 / MAXT)
           asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv1) : "f"(one_m.y));
           const float2 inv_one_m = f2(inv0, inv1);
           float2 P = f2(0.0f, 0.0f);
-  #pragma unroll
+#pragma unroll
           for (int ch = 0; ch < 3; ++ch) {
             // -q = (out - final) / (1 - aG): o - fin as fma(fin, -1, o), exact
             const float2 nq = __fmul2_rn(__ffma2_rn(fin2[ch], f2(-1.0f, -1.0f), o[ch]), inv_one_m);
@@ -1380,7 +1377,7 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 128 ? 4 : 512 / MAXT)
           const float r = warp_sum6(sc, lane);
           if ((lane & 3) == 0 && (lane >> 2) < 6 && r != 0.0f)
             atomicAdd(&s_grad[i * NV + (lane >> 2)], r);
-  #pragma unroll
+#pragma unroll
           for (int ch = 0; ch < 3; ++ch) {
             uint32_t hi, lo;
             split_half2(w[ch].x, w[ch].y, hi, lo);
@@ -1519,10 +1516,8 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 128 ? 5 : 640 / MAXT)
         const bool xin = !(fabsf(x) > h.x);
         const bool live0 = !done0 && xin && !(fabsf(y0) > h.y) && !surely_skipped(r0, al);
         const bool live1 = !done1 && xin && !(fabsf(y1) > h.y) && !surely_skipped(r1, al);
-        float e0 = gsx_expf_neg(fmaxf(-0.5f * r0, -86.0f));
-        float e1 = gsx_expf_neg(fmaxf(-0.5f * r1, -86.0f));
-        if (r0 != r0) e0 = r0;
-        if (r1 != r1) e1 = r1;
+        const float e0 = gsx_expf_nonpos(-0.5f * r0);
+        const float e1 = gsx_expf_nonpos(-0.5f * r1);
         const bool c0 = live0 && !(al * e0 < kMinRenderAlpha);
         const bool c1 = live1 && !(al * e1 < kMinRenderAlpha);
         if (!(c0 || c1)) continue;
@@ -1531,7 +1526,7 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 128 ? 5 : 640 / MAXT)
         if (isnan(coeff.x)) coeff.x = 0.0f;
         if (isnan(coeff.y)) coeff.y = 0.0f;
         const float *s = L.sh + i * GSH;
-  #pragma unroll
+#pragma unroll
         for (int ch = 0; ch < 3; ++ch) {
           float2 y;
           if constexpr (RGB) {
