@@ -14,7 +14,10 @@ device->host copy of the image, the loss and all gradients inside the timed
 region (the SH upload overlaps projection and binning, the image download
 overlaps the backward); ``roofline`` for the dominant kernel from
 per-stage CUDA events inside the timed region; ``cpu_baseline`` = the CPU
-oracle on whole steps of the same workload (median of a few).
+oracle on whole steps of the same workload (median of a few);
+``secondary_workloads`` = the batch, serve, memory and train workloads'
+own lines from shortened runs (one child process each, after the headline's
+timed region; ``--no-secondary`` skips them).
 
 ``--impl reference`` times the reference's path on the host CPU cores (the C
 restatement of its kernels in oracle/, all threads) on the same workload,
@@ -360,7 +363,45 @@ def run_gsx(args):
         line["config"]["sh_mode"] = "gaussian: one SH colour per Gaussian per view (opt-in, not the reference's images)"
     elif not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(wl, args.cpu_iters)
+    if world == 1 and args.workload == "headline" and args.sh_mode == "pixel" and not args.no_secondary:
+        line["secondary_workloads"] = secondary_workloads()
     print(json.dumps(line), flush=True)
+
+
+# The other workloads at reduced lengths, each in its own process after the
+# headline measurement: (name, extra arguments, time limit in seconds).
+SECONDARY = (
+    ("batch", ["--steps", "5", "--warmup", "3"], 300),
+    ("serve", ["--duration", "10", "--capacity-requests", "1000", "--plain-requests", "300", "--warmup", "3"], 300),
+    ("memory", ["--steps", "3", "--warmup", "3"], 300),
+    ("train", ["--steps", "20", "--warmup", "3"], 300),
+)
+
+
+def secondary_workloads() -> dict:
+    """Run every other workload of this file once, each as a child process
+    with its own time limit, and return their JSON lines by name (or the
+    reason one has none).  The headline's timed region is over by then."""
+    out = {}
+    for name, extra, limit in SECONDARY:
+        cmd = [sys.executable, os.path.abspath(__file__), "--workload", name] + extra
+        t0 = time.perf_counter()
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=limit)
+        except subprocess.TimeoutExpired:
+            out[name] = {"error": f"no line within {limit} s", "args": extra}
+            continue
+        wall = round(time.perf_counter() - t0, 1)
+        lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+        if r.returncode != 0 or not lines:
+            tail = (r.stderr or r.stdout).strip().splitlines()[-1:] or [""]
+            out[name] = {"error": f"exit {r.returncode}: {tail[0][:200]}", "args": extra, "wall_s": wall}
+            continue
+        rec = json.loads(lines[-1])
+        rec["args"] = extra
+        rec["wall_s"] = wall
+        out[name] = rec
+    return out
 
 
 def workload_config(wl, workload: str, visible: int, keys: int, world: int) -> dict:
@@ -814,6 +855,8 @@ def main():
     ap.add_argument("--no-persistent", action="store_true",
                     help="batch: one CTA per tile instead of persistent raster grids")
     ap.add_argument("--cpu-iters", type=int, default=5, help="whole CPU-oracle steps timed for cpu_baseline")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="headline: skip the shortened batch / serve / memory / train runs attached to the line")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -81,3 +81,12 @@ def test_algorithmic_bytes_per_unit():
     assert bench.algorithmic_bytes("project_bwd", n, K, P, C, T) == n * 120
     assert bench.algorithmic_bytes("binning", n, K, P, C, T) == n * 96 + K * 48 + 8 * T
     assert bench.algorithmic_bytes("unknown", n, K, P, C, T) == 0
+
+
+def test_secondary_workload_failures_are_recorded(monkeypatch):
+    """A secondary run that exits non-zero or prints no line leaves its
+    reason under its name instead of stopping the headline line."""
+    monkeypatch.setattr(bench, "SECONDARY", (("no-such-workload", ["--steps", "1"], 60),))
+    out = bench.secondary_workloads()
+    rec = out["no-such-workload"]
+    assert rec["error"].startswith("exit 2") and rec["args"] == ["--steps", "1"]
