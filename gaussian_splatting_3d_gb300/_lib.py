@@ -139,6 +139,7 @@ SIGNATURES = {
     ),
     "gsx_raster_status": (c_int, [P, c_int32, P]),
     "gsx_raster_wait_selftest": (c_int, [c_uint32, P, P]),
+    "gsx_exp_selftest": (c_int, [P, c_int64, P, c_int32, P]),
     "gsx_look_back_selftest_bytes": (c_size_t, []),
     "gsx_look_back_selftest": (c_int, [P, c_size_t, P, P]),
     "gsx_project_backward": (

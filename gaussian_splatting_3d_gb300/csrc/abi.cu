@@ -581,6 +581,14 @@ int gsx_raster_wait_selftest(uint32_t limit, uint32_t *polls_dev, void *stream) 
   return raster_wait_selftest(limit, polls_dev, as_stream(stream));
 }
 
+int gsx_exp_selftest(const float *x, int64_t n, float *out, int32_t variant, void *stream) {
+  g_err[0] = 0;
+  GSX_REQUIRE(n >= 0, "n must be >= 0");
+  GSX_REQUIRE(n == 0 || (x && out), "null input or output");
+  GSX_REQUIRE(variant >= 0 && variant <= 2, "variant must be 0, 1 or 2 (got %d)", variant);
+  return exp_selftest(x, n, out, variant, as_stream(stream));
+}
+
 int gsx_raster_status(uint32_t *flags, int32_t clear, void *stream) {
   g_err[0] = 0;
   GSX_REQUIRE(flags, "null flags pointer");

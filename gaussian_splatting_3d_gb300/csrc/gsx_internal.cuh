@@ -71,6 +71,30 @@ __device__ __forceinline__ float gsx_expf_nonpos(float x) {
   return x > -87.0f ? e : (x != x ? x : 0.0f);
 }
 
+// gsx_expf_nonpos of two values at once, every floating-point step a paired
+// float2 operation (FFMA2 / FADD2 / FMUL2 round each half exactly as the
+// scalar instruction does), so each half equals gsx_expf_nonpos bit for bit.
+__device__ __forceinline__ float2 gsx_expf_nonpos2(float2 x) {
+  const float2 xc = make_float2(fmaxf(x.x, -87.0f), fmaxf(x.y, -87.0f));
+  const float2 magic = make_float2(12582912.0f, 12582912.0f);
+  const float2 t = __ffma2_rn(xc, make_float2(1.44269502162933349609375f, 1.44269502162933349609375f), magic);
+  const float2 j = __fadd2_rn(t, make_float2(-12582912.0f, -12582912.0f));
+  float2 r = __ffma2_rn(j, make_float2(-0.693145751953125f, -0.693145751953125f), xc);
+  r = __ffma2_rn(j, make_float2(-1.428606765330187045e-06f, -1.428606765330187045e-06f), r);
+  float2 p = make_float2(1.98412698412698412e-04f, 1.98412698412698412e-04f);
+  p = __ffma2_rn(p, r, make_float2(1.38888888888888889e-03f, 1.38888888888888889e-03f));
+  p = __ffma2_rn(p, r, make_float2(8.33333333333333333e-03f, 8.33333333333333333e-03f));
+  p = __ffma2_rn(p, r, make_float2(4.16666666666666667e-02f, 4.16666666666666667e-02f));
+  p = __ffma2_rn(p, r, make_float2(1.66666666666666667e-01f, 1.66666666666666667e-01f));
+  p = __ffma2_rn(p, r, make_float2(0.5f, 0.5f));
+  p = __ffma2_rn(p, r, make_float2(1.0f, 1.0f));
+  p = __ffma2_rn(p, r, make_float2(1.0f, 1.0f));
+  const int j0 = __float_as_int(t.x) - 0x4B400000, j1 = __float_as_int(t.y) - 0x4B400000;
+  const float2 e = __fmul2_rn(p, make_float2(__int_as_float((j0 + 127) << 23), __int_as_float((j1 + 127) << 23)));
+  return make_float2(x.x > -87.0f ? e.x : (x.x != x.x ? x.x : 0.0f),
+                     x.y > -87.0f ? e.y : (x.y != x.y ? x.y : 0.0f));
+}
+
 __device__ __forceinline__ float gsx_sigmoidf(float x) {
   return 1.0f / (1.0f + gsx_expf(-x));
 }
@@ -266,6 +290,10 @@ int raster_status(uint32_t *flags, int clear, cudaStream_t s);
 // One CTA waits on a barrier phase that cannot complete, for `limit` polls;
 // sets the raster timeout bit and writes the polls made to polls_dev[0].
 int raster_wait_selftest(uint32_t limit, uint32_t *polls_dev, cudaStream_t s);
+
+// out[i] = gsx_expf (variant 0), gsx_expf_nonpos (1) or gsx_expf_nonpos2 on
+// the pairs (x[2k], x[2k+1]) (2) of x[i], for i < n.
+int exp_selftest(const float *x, int64_t n, float *out, int variant, cudaStream_t s);
 
 // Binning.  rect_tl/rect_br point at int32 pairs with `rect_stride` ints per
 // Gaussian (4 for packed [n,4] rects, 2 for separate [n,2] arrays).

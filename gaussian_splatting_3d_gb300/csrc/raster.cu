@@ -1287,26 +1287,34 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 128 ? 4 : 512 / MAXT)
           // both pixels' decision paths side by side, without branches: the
           // radial of gs/src/include/kernels.h:172-187 (one det per Gaussian,
           // IEEE division), then the exact exponential where it can decide
+          // The two pixels share x (same column); every other step runs as
+          // a paired float2 operation, each half rounded as its scalar form
+          // (-(y*z) == y*(-z) and a - b == a + (-b) exactly).
           const float2 h = L.box[i];
-          const float x = px - m.x, y0 = py0 - m.y, y1 = py1 - m.y;
+          const float x = px - m.x;
+          const float2 y = __fadd2_rn(f2(py0, py1), f2(-m.y, -m.y));
+          const float2 X = f2(x, x);
           const float det = fmaf(cv.x, cv.w, -(cv.y * cv.z));
-          tx_0 = fmaf(x, cv.w, -(y0 * cv.z));
-          ty_0 = fmaf(-x, cv.y, y0 * cv.x);
-          tx_1 = fmaf(x, cv.w, -(y1 * cv.z));
-          ty_1 = fmaf(-x, cv.y, y1 * cv.x);
-          float r0 = fmaf(tx_0, x, ty_0 * y0) / det;
-          float r1 = fmaf(tx_1, x, ty_1 * y1) / det;
+          const float2 txp = __ffma2_rn(X, f2(cv.w, cv.w), __fmul2_rn(y, f2(-cv.z, -cv.z)));
+          const float2 typ = __ffma2_rn(f2(-x, -x), f2(cv.y, cv.y), __fmul2_rn(y, f2(cv.x, cv.x)));
+          tx_0 = txp.x;
+          tx_1 = txp.y;
+          ty_0 = typ.x;
+          ty_1 = typ.y;
+          const float2 num = __ffma2_rn(txp, X, __fmul2_rn(typ, y));
+          float r0 = num.x / det;
+          float r1 = num.y / det;
           if (r0 < 0.0f) r0 = 1000.0f;
           if (r1 < 0.0f) r1 = 1000.0f;
           const bool xin = !(fabsf(x) > h.x);
-          const bool live0 = !done0 && xin && !(fabsf(y0) > h.y) && !surely_skipped(r0, al);
-          const bool live1 = !done1 && xin && !(fabsf(y1) > h.y) && !surely_skipped(r1, al);
-          const float e0 = gsx_expf_nonpos(-0.5f * r0);
-          const float e1 = gsx_expf_nonpos(-0.5f * r1);
-              c0 = live0 && !(al * e0 < kMinRenderAlpha);
-          c1 = live1 && !(al * e1 < kMinRenderAlpha);
-          G0 = c0 ? e0 : 0.0f;
-          G1 = c1 ? e1 : 0.0f;
+          const bool live0 = !done0 && xin && !(fabsf(y.x) > h.y) && !surely_skipped(r0, al);
+          const bool live1 = !done1 && xin && !(fabsf(y.y) > h.y) && !surely_skipped(r1, al);
+          const float2 e = gsx_expf_nonpos2(__fmul2_rn(f2(-0.5f, -0.5f), f2(r0, r1)));
+          const float2 ae = __fmul2_rn(f2(al, al), e);
+          c0 = live0 && !(ae.x < kMinRenderAlpha);
+          c1 = live1 && !(ae.y < kMinRenderAlpha);
+          G0 = c0 ? e.x : 0.0f;
+          G1 = c1 ? e.y : 0.0f;
         }
         float sc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
         float2 w[3] = {f2(0.0f, 0.0f), f2(0.0f, 0.0f), f2(0.0f, 0.0f)};
@@ -1507,21 +1515,27 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 128 ? 5 : 640 / MAXT)
         const float4 cv = L.cov[i];
         const float2 m = L.mean[i];
         const float2 h = L.box[i];
-        const float x = px - m.x, y0 = py0 - m.y, y1 = py1 - m.y;
+        // paired float2 steps, each half rounded as in the one-pixel kernel
+        const float x = px - m.x;
+        const float2 y = __fadd2_rn(f2(py0, py1), f2(-m.y, -m.y));
+        const float2 X = f2(x, x);
         const float det = fmaf(cv.x, cv.w, -(cv.y * cv.z));
-        float r0 = fmaf(fmaf(x, cv.w, -(y0 * cv.z)), x, fmaf(-x, cv.y, y0 * cv.x) * y0) / det;
-        float r1 = fmaf(fmaf(x, cv.w, -(y1 * cv.z)), x, fmaf(-x, cv.y, y1 * cv.x) * y1) / det;
+        const float2 txp = __ffma2_rn(X, f2(cv.w, cv.w), __fmul2_rn(y, f2(-cv.z, -cv.z)));
+        const float2 typ = __ffma2_rn(f2(-x, -x), f2(cv.y, cv.y), __fmul2_rn(y, f2(cv.x, cv.x)));
+        const float2 num = __ffma2_rn(txp, X, __fmul2_rn(typ, y));
+        float r0 = num.x / det;
+        float r1 = num.y / det;
         if (r0 < 0.0f) r0 = 1000.0f;
         if (r1 < 0.0f) r1 = 1000.0f;
         const bool xin = !(fabsf(x) > h.x);
-        const bool live0 = !done0 && xin && !(fabsf(y0) > h.y) && !surely_skipped(r0, al);
-        const bool live1 = !done1 && xin && !(fabsf(y1) > h.y) && !surely_skipped(r1, al);
-        const float e0 = gsx_expf_nonpos(-0.5f * r0);
-        const float e1 = gsx_expf_nonpos(-0.5f * r1);
-        const bool c0 = live0 && !(al * e0 < kMinRenderAlpha);
-        const bool c1 = live1 && !(al * e1 < kMinRenderAlpha);
+        const bool live0 = !done0 && xin && !(fabsf(y.x) > h.y) && !surely_skipped(r0, al);
+        const bool live1 = !done1 && xin && !(fabsf(y.y) > h.y) && !surely_skipped(r1, al);
+        const float2 e = gsx_expf_nonpos2(__fmul2_rn(f2(-0.5f, -0.5f), f2(r0, r1)));
+        const float2 ae = __fmul2_rn(f2(al, al), e);
+        const bool c0 = live0 && !(ae.x < kMinRenderAlpha);
+        const bool c1 = live1 && !(ae.y < kMinRenderAlpha);
         if (!(c0 || c1)) continue;
-        const float2 Gp = f2(c0 ? e0 : 0.0f, c1 ? e1 : 0.0f);
+        const float2 Gp = f2(c0 ? e.x : 0.0f, c1 ? e.y : 0.0f);
         float2 coeff = __fmul2_rn(__fmul2_rn(f2(al, al), T2), Gp);
         if (isnan(coeff.x)) coeff.x = 0.0f;
         if (isnan(coeff.y)) coeff.y = 0.0f;
@@ -1974,6 +1988,35 @@ int launch_raster_forward_batch(const RasterArgs &a, int C, int64_t total_tiles,
 int launch_raster_backward_batch(const RasterArgs &a, int C, int64_t total_tiles, cudaStream_t s) {
   if (total_tiles == 0) return GSX_OK;
   return dispatch_bwd<true>(a, C, total_tiles, s);
+}
+
+__global__ void exp_selftest_kernel(const float *__restrict__ x, int64_t n, float *__restrict__ out,
+                                    int variant) {
+  const int64_t i = 2 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+  if (i >= n) return;
+  const float a = x[i], b = i + 1 < n ? x[i + 1] : 0.0f;
+  float ra, rb;
+  if (variant == 0) {
+    ra = gsx_expf(a);
+    rb = gsx_expf(b);
+  } else if (variant == 1) {
+    ra = gsx_expf_nonpos(a);
+    rb = gsx_expf_nonpos(b);
+  } else {
+    const float2 r = gsx_expf_nonpos2(make_float2(a, b));
+    ra = r.x;
+    rb = r.y;
+  }
+  out[i] = ra;
+  if (i + 1 < n) out[i + 1] = rb;
+}
+
+int exp_selftest(const float *x, int64_t n, float *out, int variant, cudaStream_t s) {
+  if (n <= 0) return GSX_OK;
+  const int64_t pairs = (n + 1) / 2;
+  count_launches(1);
+  exp_selftest_kernel<<<(unsigned)((pairs + 255) / 256), 256, 0, s>>>(x, n, out, variant);
+  return cuda_status(cudaGetLastError(), "exp_selftest_kernel launch");
 }
 
 int raster_wait_selftest(uint32_t limit, uint32_t *polls_dev, cudaStream_t s) {

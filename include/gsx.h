@@ -440,6 +440,16 @@ int gsx_raster_status(uint32_t *flags, int32_t clear, void *stream);
  */
 int gsx_raster_wait_selftest(uint32_t limit, uint32_t *polls_dev, void *stream);
 
+/*
+ * Diagnostic of the raster's exponential (no reference counterpart; the
+ * reference calls CUDA's expf at gs/src/include/kernels.h:188): out[i] for
+ * x[i], i < n, both device memory, through the scalar form used by the
+ * projection and the CPU oracle (variant 0), the branch-free form for
+ * exponents <= 0 of the raster kernels (1), or its paired float2 form on
+ * (x[2k], x[2k+1]) (2).  Enqueued on `stream`.
+ */
+int gsx_exp_selftest(const float *x, int64_t n, float *out, int32_t variant, void *stream);
+
 /* gsx_render_backward with CTA b working on tile tile_order[b] (the same
  * contract as gsx_render_forward_ordered; the gradients do not depend on the
  * order beyond the summation order of their float additions). */
