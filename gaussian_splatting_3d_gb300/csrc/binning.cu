@@ -105,6 +105,8 @@ __global__ void __launch_bounds__(kThreads)
                      uint32_t *__restrict__ hist) {
   constexpr uint32_t RADIX = 1u << RB, MASK = RADIX - 1u;
   __shared__ uint32_t sh[4 * 256];  // passes * RADIX <= 1024
+  pdl_wait();
+  pdl_trigger();
   const uint32_t n = n_dev ? min(*n_dev, n_max) : n_max;
   for (int i = threadIdx.x; i < 4 * 256; i += kThreads) sh[i] = 0;
   __syncthreads();
@@ -135,6 +137,8 @@ __global__ void __launch_bounds__(kThreads)
   constexpr int DPT = (int)RADIX / kThreads;  // digits per thread
   constexpr int TILE = kThreads * ITEMS;
   static_assert(DPT >= 1 && DPT * kThreads == (int)RADIX, "RADIX must be a multiple of kThreads");
+  pdl_wait();
+  pdl_trigger();
   const uint32_t n = n_dev ? min(*n_dev, n_max) : n_max;
   __shared__ uint32_t s_warp[kWarps][RADIX];
   __shared__ uint32_t s_cta_excl[RADIX];
@@ -297,6 +301,8 @@ __global__ void __launch_bounds__(kThreads)
   __shared__ uint32_t s_g[kWarps][32], s_tb[kWarps][32];
   __shared__ int32_t s_x0[kWarps][32], s_y0[kWarps][32], s_w[kWarps][32], s_ntw[kWarps][32];
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  pdl_wait();
+  pdl_trigger();
   if (t == 0) s_chunk = atomicAdd(chunk_counter, 1u);
   __syncthreads();
   const uint32_t chunk = s_chunk;
@@ -463,6 +469,8 @@ __global__ void __launch_bounds__(kThreads)
 __global__ void ranges_kernel(const uint32_t *__restrict__ tiles, const uint32_t *__restrict__ K_dev,
                               uint32_t n_tiles, int32_t *__restrict__ start,
                               int32_t *__restrict__ end) {
+  pdl_wait();
+  pdl_trigger();
   const uint32_t K = *K_dev;
   const uint32_t base = 4u * (blockIdx.x * blockDim.x + threadIdx.x);
   if (base >= K) return;
@@ -572,11 +580,9 @@ int radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t n_max,
   uint32_t hist_grid = (n_max + kThreads * 16 - 1) / (kThreads * 16);
   if (hist_grid > 1024u) hist_grid = 1024u;
   count_launches(1);
-  if (rb == 9)
-    histogram_kernel<9><<<hist_grid, kThreads, 0, s>>>(keys_in, n_max, n_dev, passes, hist);
-  else
-    histogram_kernel<8><<<hist_grid, kThreads, 0, s>>>(keys_in, n_max, n_dev, passes, hist);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e =
+      rb == 9 ? launch_pdl(histogram_kernel<9>, hist_grid, kThreads, 0, s, keys_in, n_max, n_dev, passes, hist)
+              : launch_pdl(histogram_kernel<8>, hist_grid, kThreads, 0, s, keys_in, n_max, n_dev, passes, hist);
   if (e != cudaSuccess) return cuda_status(e, "histogram_kernel launch");
   const uint32_t tile = kThreads * (rb == 9 ? kItems9 : kItems);
   const uint32_t chunks = (n_max + tile - 1) / tile;
@@ -593,13 +599,10 @@ int radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t n_max,
     uint32_t *vo = last ? final_vals : scratch_v[p & 1];
     uint32_t *st = status + (size_t)chunks * radix * p;
     count_launches(1);
-    if (rb == 9)
-      onesweep_kernel<9, kItems9><<<chunks, kThreads, 0, s>>>(
-          ki, vi, ko, vo, n_max, n_dev, rb * p, hist + radix * p, st, tickets + p, error);
-    else
-      onesweep_kernel<8, kItems><<<chunks, kThreads, 0, s>>>(
-          ki, vi, ko, vo, n_max, n_dev, rb * p, hist + radix * p, st, tickets + p, error);
-    e = cudaGetLastError();
+    e = rb == 9 ? launch_pdl(onesweep_kernel<9, kItems9>, chunks, kThreads, 0, s, ki, vi, ko, vo, n_max, n_dev,
+                             rb * p, hist + radix * p, st, tickets + p, error)
+                : launch_pdl(onesweep_kernel<8, kItems>, chunks, kThreads, 0, s, ki, vi, ko, vo, n_max, n_dev,
+                             rb * p, hist + radix * p, st, tickets + p, error);
     if (e != cudaSuccess) return cuda_status(e, "onesweep_kernel launch");
     ki = ko;
     vi = vo;
@@ -705,12 +708,9 @@ int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
   // 2. scan of counts + emission
   const uint32_t emit_chunks = (nn + kEmitTile - 1) / kEmitTile;
   count_launches(1);
-  emit_kernel<<<emit_chunks, kThreads, 0, s>>>(
-      w.dvals[1], nn, rect_tl, rect_br, rect_stride, counts, n_tiles_w, n_tiles_h, views, n_views,
-      w.tkeys[0],
-      w.tvals[0], (unsigned long long)capacity, w.emit_status, w.counters + 8, w.total, w.k_eff,
-      w.error);
-  e = cudaGetLastError();
+  e = launch_pdl(emit_kernel, emit_chunks, kThreads, 0, s, w.dvals[1], nn, rect_tl, rect_br, rect_stride, counts,
+                 n_tiles_w, n_tiles_h, views, n_views, w.tkeys[0], w.tvals[0], (unsigned long long)capacity,
+                 w.emit_status, w.counters + 8, w.total, w.k_eff, w.error);
   if (e != cudaSuccess) return cuda_status(e, "emit_kernel launch");
   if (capacity == 0) return GSX_OK;
   const uint32_t cap = (uint32_t)capacity;
@@ -733,9 +733,8 @@ int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
   }
   // 4. start / end
   count_launches(1);
-  ranges_kernel<<<(cap + 1023) / 1024, 256, 0, s>>>(final_keys, w.k_eff, (uint32_t)n_tiles, start,
-                                                     end);
-  e = cudaGetLastError();
+  e = launch_pdl(ranges_kernel, (cap + 1023) / 1024, 256, 0, s, final_keys, w.k_eff, (uint32_t)n_tiles, start,
+                 end);
   if (e != cudaSuccess) return cuda_status(e, "ranges_kernel launch");
   return GSX_OK;
 }

@@ -115,6 +115,47 @@ __device__ __forceinline__ bool sphere_in_frustum(float mx, float my, float mz,
   return true;
 }
 
+// ---- programmatic dependent launch ----------------------------------------
+// A kernel launched by launch_pdl may be scheduled while the previous kernel
+// on its stream is still finishing (its launch and CTA set-up overlap that
+// kernel's last wave).  Every such kernel calls pdl_wait() before it reads or
+// writes anything: the wait returns once the previous kernel has completed
+// and its memory operations are visible, so the stream order of the results
+// is unchanged.  pdl_trigger() right after the wait lets the next kernel be
+// scheduled in turn.  Both are no-ops for a kernel launched without the
+// attribute.
+#ifndef GSX_PDL
+#define GSX_PDL 1
+#endif
+
+__device__ __forceinline__ void pdl_wait() {
+#if GSX_PDL
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
+}
+
+__device__ __forceinline__ void pdl_trigger() {
+#if GSX_PDL
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
+}
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                       Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = GSX_PDL ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // ---- bulk copies (the TMA engine) and mbarriers ----------------------------
 // cp.async.bulk global -> shared completing on an mbarrier; every wait on a
 // barrier phase is bounded (kBulkWaitLimit polls), after which the caller
