@@ -9,6 +9,8 @@
 // host gives the sizes, so no entry point reads device memory to plan.
 #include <cstring>
 
+#include <algorithm>
+
 #include "gsx_internal.cuh"
 
 using namespace gsx;
@@ -142,9 +144,12 @@ int gsx_batch_bin_async(const gsx_batch_view *views_dev, const gsx_batch_view *v
     set_error("null pointer argument");
     return GSX_ERR_INVALID_ARG;
   }
+  int64_t max_view_tiles = 0;  // the largest view's tile count: the width of the local tile ids
+  for (int32_t i = 0; i < n_views; ++i)
+    max_view_tiles = std::max(max_view_tiles, (int64_t)views_host[i].n_tiles_w * views_host[i].n_tiles_h);
   return run_binning_async(b.n_items, rect, rect + 2, 4, counts, depth, 0, 0, key_capacity,
                            gaussian_ids, start, end, workspace, workspace_bytes,
-                           as_stream(stream), views_dev, n_views, b.total_tiles);
+                           as_stream(stream), views_dev, n_views, b.total_tiles, max_view_tiles);
 }
 
 int gsx_batch_render_forward(const gsx_batch_view *views_dev, const gsx_batch_view *views_host,

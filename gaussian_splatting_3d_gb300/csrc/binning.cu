@@ -22,6 +22,8 @@
 // shared memory so that the global writes are runs of consecutive addresses.
 // Every wait on a predecessor is bounded; on expiry an error word is set and
 // the host returns GSX_ERR_TIMEOUT.
+#include <algorithm>
+
 #include "gsx_internal.cuh"
 
 namespace gsx {
@@ -274,6 +276,37 @@ __device__ __forceinline__ long long rect_count(const int32_t *tl, const int32_t
   return c < (1ll << 31) ? c : (1ll << 31);
 }
 
+// Makes the depth order of a batch view-major: writes the view of every item
+// in depth order as the key of one more stable pass, and clears the state
+// that pass reuses from the first depth pass (its histogram row, chunk ticket
+// and look-back rows), which the depth sort no longer needs.
+__global__ void __launch_bounds__(kThreads)
+    view_keys_kernel(const uint32_t *__restrict__ order, uint32_t n,
+                     const gsx_batch_view *__restrict__ views, int32_t n_views,
+                     uint32_t *__restrict__ vkeys, uint32_t *__restrict__ hist_row,
+                     uint32_t *__restrict__ rows, uint32_t row_words, uint32_t *__restrict__ ticket) {
+  __shared__ long long s_off[256];  // item offsets of the views (n_views <= 256)
+  pdl_wait();
+  pdl_trigger();
+  for (int v = threadIdx.x; v < n_views; v += blockDim.x) s_off[v] = views[v].item_offset;
+  __syncthreads();
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
+  for (uint32_t i = first; i < n; i += stride) {
+    const long long g = order[i];
+    int lo = 0, hi = n_views - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (s_off[mid] <= g) lo = mid;
+      else hi = mid - 1;
+    }
+    vkeys[i] = (uint32_t)lo;
+  }
+  for (uint32_t i = first; i < row_words; i += stride) rows[i] = 0u;
+  if (first < 256) hist_row[first] = 0u;
+  if (first == 0) *ticket = 0u;
+}
+
 // Exclusive scan of key counts in depth order (decoupled look-back over
 // chunks of kEmitTile = 512 Gaussians) fused with the emission of (tile,
 // Gaussian) pairs.  Warp w of a chunk owns its items w*64 + j*32 + lane
@@ -292,7 +325,7 @@ __global__ void __launch_bounds__(kThreads)
                 uint32_t *__restrict__ tile_out, uint32_t *__restrict__ id_out,
                 unsigned long long capacity, unsigned long long *status,
                 uint32_t *chunk_counter, unsigned long long *total_out, uint32_t *k_eff,
-                uint32_t *error) {
+                uint32_t *error, int view_shift) {
   __shared__ unsigned long long s_tmp[kWarps];
   __shared__ unsigned long long s_prefix;
   __shared__ uint32_t s_chunk;
@@ -419,7 +452,8 @@ __global__ void __launch_bounds__(kThreads)
         }
         ntw = views[lo].n_tiles_w;
         nth = views[lo].n_tiles_h;
-        tb = (uint32_t)views[lo].tile_offset;
+        // global tile ids, or (view << view_shift) | local tile in view-major mode
+        tb = view_shift ? (uint32_t)lo << view_shift : (uint32_t)views[lo].tile_offset;
       }
       const bool in_grid = tl[0] >= 0 && tl[1] >= 0 && br[0] < ntw && br[1] < nth;
       if (!in_grid) atomicOr(error, kErrRange);
@@ -466,9 +500,23 @@ __global__ void __launch_bounds__(kThreads)
 // start/end of every tile from the sorted tile ids: 4 consecutive keys per
 // thread (one 16-byte load; `tiles` is 16-byte aligned), their neighbours
 // from the adjacent threads' loads or, at warp edges, from memory.
+// In view-major mode (view_shift > 0) a key is (view << view_shift) | local
+// tile and the range goes to the view's global tile tile_offset + local.
+__device__ __forceinline__ uint32_t range_slot(uint32_t key, uint32_t n_tiles,
+                                               const gsx_batch_view *views, int32_t n_views,
+                                               int view_shift) {
+  if (!view_shift) return key < n_tiles ? key : 0xffffffffu;
+  const uint32_t v = key >> view_shift, t = key & ((1u << view_shift) - 1u);
+  if (v >= (uint32_t)n_views) return 0xffffffffu;
+  const gsx_batch_view &vw = views[v];
+  if ((int64_t)t >= (int64_t)vw.n_tiles_w * vw.n_tiles_h) return 0xffffffffu;
+  return (uint32_t)(vw.tile_offset + t);
+}
+
 __global__ void ranges_kernel(const uint32_t *__restrict__ tiles, const uint32_t *__restrict__ K_dev,
                               uint32_t n_tiles, int32_t *__restrict__ start,
-                              int32_t *__restrict__ end) {
+                              int32_t *__restrict__ end, const gsx_batch_view *__restrict__ views,
+                              int32_t n_views, int view_shift) {
   pdl_wait();
   pdl_trigger();
   const uint32_t K = *K_dev;
@@ -492,11 +540,14 @@ __global__ void ranges_kernel(const uint32_t *__restrict__ tiles, const uint32_t
     const uint32_t i = base + j;
     if (i >= K) break;
     const uint32_t t = v[j];
-    if (t >= n_tiles) continue;
     const uint32_t before = j == 0 ? prev : v[j - 1];
     const uint32_t after = j == 3 ? next : v[j + 1];
-    if (i == 0 || before != t) start[t] = (int32_t)i;
-    if (i == K - 1 || after != t) end[t] = (int32_t)(i + 1);
+    const bool first_key = i == 0 || before != t, last_key = i == K - 1 || after != t;
+    if (!first_key && !last_key) continue;
+    const uint32_t slot = range_slot(t, n_tiles, views, n_views, view_shift);
+    if (slot == 0xffffffffu) continue;
+    if (first_key) start[slot] = (int32_t)i;
+    if (last_key) end[slot] = (int32_t)(i + 1);
   }
 }
 
@@ -674,7 +725,8 @@ int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
                       int32_t rect_stride, const int32_t *counts, const float *depth,
                       int32_t n_tiles_w, int32_t n_tiles_h, int64_t capacity, int32_t *ids,
                       int32_t *start, int32_t *end, void *ws, size_t ws_bytes, cudaStream_t s,
-                      const gsx_batch_view *views, int32_t n_views, int64_t total_tiles) {
+                      const gsx_batch_view *views, int32_t n_views, int64_t total_tiles,
+                      int64_t max_view_tiles) {
   const int64_t n_tiles = views ? total_tiles : (int64_t)n_tiles_w * n_tiles_h;
   Workspace w = carve_ws(ws, n, capacity);
   if (ws_bytes < w.bytes) {
@@ -685,7 +737,18 @@ int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
     set_error("binning workspace must be 256-byte aligned");
     return GSX_ERR_INVALID_ARG;
   }
-  const int tile_bits = bits_for((uint64_t)(n_tiles > 0 ? n_tiles - 1 : 0));
+  // View-major batches (up to 256 views): one more stable pass orders the
+  // depth-sorted items by view, the emitted keys are (view << view_shift) |
+  // local tile, and the tile sort needs only the local bits (two 8-bit passes
+  // for 1080p views at 16x16 instead of two 9-bit passes over the global ids):
+  // a stable sort of view-major keys on their low bits keeps each (view, tile)
+  // list contiguous and in depth order.
+  int view_shift = 0;
+  if (views && n_views <= 256 && max_view_tiles > 0) {
+    const int lb = std::max(1, bits_for((uint64_t)(max_view_tiles - 1)));
+    if (lb + bits_for((uint64_t)(n_views - 1)) <= 31) view_shift = lb;
+  }
+  const int tile_bits = view_shift ? view_shift : bits_for((uint64_t)(n_tiles > 0 ? n_tiles - 1 : 0));
   const int tile_passes = tile_bits == 0 ? 0 : sort_passes(tile_bits);
   // one clear of the zero-initialised state, through the last tile pass in
   // use (a pass's rows are packed: chunks x 2^digit_bits words)
@@ -705,12 +768,30 @@ int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
                       w.dkeys[1], w.dvals[1], w.hist, w.counters, w.status_depth, w.depth_chunks,
                       w.error, s);
   if (st != GSX_OK) return st;
+  const uint32_t *order = w.dvals[1];
+  if (view_shift && n_views > 1) {
+    // 1b. stable pass on the view of each item: (view, depth) order.  The
+    // depth sort's first-pass state (histogram row, ticket, look-back rows)
+    // is cleared by view_keys_kernel and reused; keys in dkeys[0], result in
+    // dvals[0] (its keys in dkeys[1]).
+    const uint32_t rows = (uint32_t)(((nn + kTile - 1) / kTile) * 256);
+    const uint32_t grid = std::min<uint32_t>((nn + kThreads - 1) / kThreads, 4096u);
+    count_launches(1);
+    e = launch_pdl(view_keys_kernel, std::max(grid, 1u), kThreads, 0, s, (const uint32_t *)w.dvals[1], nn, views,
+                   n_views, w.dkeys[0], w.hist, w.status_depth, rows, w.counters);
+    if (e != cudaSuccess) return cuda_status(e, "view_keys_kernel launch");
+    uint32_t *vk[2] = {w.dkeys[1], w.dkeys[1]}, *vv[2] = {w.dvals[0], w.dvals[0]};  // one pass: unused
+    st = radix_sort(w.dkeys[0], w.dvals[1], nn, nullptr, bits_for((uint64_t)(n_views - 1)), vk, vv, w.dkeys[1],
+                    w.dvals[0], w.hist, w.counters, w.status_depth, w.depth_chunks, w.error, s);
+    if (st != GSX_OK) return st;
+    order = w.dvals[0];
+  }
   // 2. scan of counts + emission
   const uint32_t emit_chunks = (nn + kEmitTile - 1) / kEmitTile;
   count_launches(1);
-  e = launch_pdl(emit_kernel, emit_chunks, kThreads, 0, s, w.dvals[1], nn, rect_tl, rect_br, rect_stride, counts,
+  e = launch_pdl(emit_kernel, emit_chunks, kThreads, 0, s, order, nn, rect_tl, rect_br, rect_stride, counts,
                  n_tiles_w, n_tiles_h, views, n_views, w.tkeys[0], w.tvals[0], (unsigned long long)capacity,
-                 w.emit_status, w.counters + 8, w.total, w.k_eff, w.error);
+                 w.emit_status, w.counters + 8, w.total, w.k_eff, w.error, view_shift);
   if (e != cudaSuccess) return cuda_status(e, "emit_kernel launch");
   if (capacity == 0) return GSX_OK;
   const uint32_t cap = (uint32_t)capacity;
@@ -734,7 +815,7 @@ int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
   // 4. start / end
   count_launches(1);
   e = launch_pdl(ranges_kernel, (cap + 1023) / 1024, 256, 0, s, final_keys, w.k_eff, (uint32_t)n_tiles, start,
-                 end);
+                 end, views, n_views, view_shift);
   if (e != cudaSuccess) return cuda_status(e, "ranges_kernel launch");
   return GSX_OK;
 }

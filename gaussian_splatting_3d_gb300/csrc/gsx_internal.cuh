@@ -344,7 +344,7 @@ int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
                       int32_t n_tiles_w, int32_t n_tiles_h, int64_t capacity, int32_t *ids,
                       int32_t *start, int32_t *end, void *ws, size_t ws_bytes, cudaStream_t s,
                       const gsx_batch_view *views = nullptr, int32_t n_views = 0,
-                      int64_t total_tiles = 0);
+                      int64_t total_tiles = 0, int64_t max_view_tiles = 0);
 int binning_status(const void *ws, int64_t n, int64_t capacity, int32_t n_tiles_w,
                    int32_t n_tiles_h, int64_t *n_keys_host, uint32_t *flags_host, cudaStream_t s);
 int copy_binning_status_async(const void *ws, int64_t n, int64_t capacity, void *dst,

@@ -14,7 +14,7 @@ torch = pytest.importorskip("torch")
 
 from gaussian_splatting_3d_gb300 import batch as B  # noqa: E402
 from gaussian_splatting_3d_gb300 import renderer, scene as S  # noqa: E402
-from gaussian_splatting_3d_gb300.camera import CameraInfo, look_at_c2w  # noqa: E402
+from gaussian_splatting_3d_gb300.camera import CameraInfo, look_at_c2w, make_gsx_camera  # noqa: E402
 
 pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("raster_flags_clean")]
 GRAD_REL = 1e-4
@@ -144,9 +144,9 @@ def test_batched_schedules_give_the_same_images_and_close_gradients():
 
 
 def test_batch_with_more_than_65536_tiles_matches_per_view():
-    """9 views of 1920x1080 at 16x16 tiles: 73,440 tiles, so the batched tile
-    ids take 17 bits and the tile sort runs two 9-bit passes; every image
-    must still equal the view rendered alone."""
+    """9 views of 1920x1080 at 16x16 tiles: 73,440 tiles, so the global tile
+    ids (start/end) take 17 bits while the view-major tile sort runs on the
+    13 local bits; every image must still equal the view rendered alone."""
     sc = S.custom_workload(3000, 64, 64, 3, seed=37).scene
     scene_t = B.Scene.from_arrays(sc, dev())
     views = make_views(9, seed=37, sizes=((1920, 1080),))
@@ -186,3 +186,59 @@ def test_persistent_raster_matches_one_cta_per_tile():
         np.testing.assert_array_equal(a, b)
     for a, b in zip(runs[0][1], runs[1][1]):
         assert np.abs(a - b).max() <= 1e-4 * max(np.abs(b).max(), 1e-3)
+
+
+def batch_lists(bp, tables):
+    """Per view and tile: the batch's list as the view's Gaussian ids."""
+    ids, start, end = bp.ids.cpu().numpy(), bp.start.cpu().numpy(), bp.end.cpu().numpy()
+    out = []
+    for e in tables:
+        lists = {}
+        for t in range(e.n_tiles_w * e.n_tiles_h):
+            g = e.tile_offset + t
+            if start[g] >= 0:
+                lists[t] = ids[start[g]:end[g]] - e.item_offset
+        out.append(lists)
+    return out
+
+
+def test_batch_lists_equal_the_views_own_lists():
+    """The view-major batched binning (items ordered by (view, depth), keys
+    (view << shift) | local tile, sorted on the local bits) gives every tile
+    of every view exactly the list the single-view binning gives it: same
+    Gaussians, same depth order."""
+    sc = S.custom_workload(6000, 64, 64, 3, seed=71).scene
+    scene_t = B.Scene.from_arrays(sc, dev())
+    views = make_views(6, seed=72, sizes=((160, 90), (96, 80), (128, 128)))
+    st = renderer.RasterSettings()
+    bp = B.BatchPipeline(dev(), st).plan([scene_t], [B.ViewSpec(0, c, cam) for c, cam in views], backward=False)
+    bp.forward()
+    torch.cuda.synchronize()
+    got = batch_lists(bp, [bp.table[i] for i in range(len(views))])
+    for i, (c2w, cam) in enumerate(views):
+        pr = renderer.project(scene_t.mean, scene_t.qvec, scene_t.log_scale, scene_t.alpha_logit,
+                              make_gsx_camera(c2w, cam), st)
+        ntw, nth = st.tiles(cam)
+        ids, start, end, K = renderer.bin_gaussians(pr, ntw, nth)
+        ids, start, end = ids.cpu().numpy(), start.cpu().numpy(), end.cpu().numpy()
+        want = {t: ids[start[t]:end[t]] for t in range(ntw * nth) if start[t] >= 0}
+        assert set(got[i]) == set(want), i
+        for t in want:
+            np.testing.assert_array_equal(got[i][t], want[t], err_msg=f"view {i} tile {t}")
+
+
+def test_batch_of_257_views_takes_global_tile_keys():
+    """More than 256 views: the binning keeps global tile ids (no view-major
+    pass); images still equal the views rendered alone."""
+    sc = S.custom_workload(1500, 64, 64, 3, seed=73).scene
+    scene_t = B.Scene.from_arrays(sc, dev())
+    views = make_views(257, seed=74, sizes=((32, 32), (48, 32)))
+    st = renderer.RasterSettings()
+    bp = B.BatchPipeline(dev(), st).plan([scene_t], [B.ViewSpec(0, c, cam) for c, cam in views], backward=False)
+    bp.forward()
+    torch.cuda.synchronize()
+    params = [scene_t.mean, scene_t.qvec, scene_t.log_scale, scene_t.sh, scene_t.alpha_logit]
+    for i in range(0, 257, 16):
+        c2w, cam = views[i]
+        img = renderer.rasterize(*params, c2w, cam, st)
+        np.testing.assert_array_equal(bp.images[i].cpu().numpy(), img.cpu().numpy())
