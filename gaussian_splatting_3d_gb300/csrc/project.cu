@@ -240,16 +240,91 @@ struct Frame {
   float M[3][3];
 };
 
+// ---- the backward's rotation in float-float ---------------------------------
+// The quaternion gradient of a needle-like Gaussian is a small difference of
+// large terms (dL/dSigma of order 1e6 against M's thin columns), so it is
+// only as accurate as R: R in float (a few ulp per entry) moves dL/dq by
+// ~1e-4 of the tensor's largest entry against an exact evaluation, while R
+// exact to ~2^-44 and rounded once into M = R diag(s) leaves ~2e-5 (the
+// other float stages' share).  R is formed as N / |q|^2 (N the quadratic form
+// of the unnormalised quaternion, equal to the normalised formula) with the
+// error-free transformations two-product (FMA) and two-sum (Knuth), and a
+// Newton-refined reciprocal.  The forward keeps the float R of quat_rot,
+// whose rounding the rendered covariance reproduces bit for bit.
+struct FF {
+  float hi, lo;
+};
+
+__device__ __forceinline__ FF ff_prod(float a, float b) {
+  const float p = a * b;
+  return {p, fmaf(a, b, -p)};
+}
+
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  const float e = (a.hi - (s - bb)) + (b.hi - bb);
+  const float lo = e + (a.lo + b.lo);
+  const float hi = s + lo;
+  return {hi, lo - (hi - s)};
+}
+
+__device__ __forceinline__ FF ff_sub(FF a, FF b) { return ff_add(a, {-b.hi, -b.lo}); }
+
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+  const FF p = ff_prod(a.hi, b.hi);
+  const float lo = fmaf(a.hi, b.lo, a.lo * b.hi) + p.lo;
+  const float hi = p.hi + lo;
+  return {hi, lo - (hi - p.hi)};
+}
+
+// R(q / |q|) in float-float; false (R untouched) for |q| below the 1e-12 clamp.
+__device__ __forceinline__ bool quat_rot_ff(const float4 q, FF (&R)[3][3]) {
+  const float w = q.x, x = q.y, y = q.z, z = q.w;
+  const FF ww = ff_prod(w, w), xx = ff_prod(x, x), yy = ff_prod(y, y), zz = ff_prod(z, z);
+  const FF n2 = ff_add(ff_add(ww, xx), ff_add(yy, zz));
+  if (!(n2.hi >= 1e-24f)) return false;
+  const float r0 = 1.0f / n2.hi;
+  const float e = fmaf(-n2.hi, r0, 1.0f) - n2.lo * r0;  // 1 - |q|^2 r0
+  const FF inv = {r0, r0 * e};
+  const FF xy = ff_prod(x, y), wz = ff_prod(w, z), xz = ff_prod(x, z), wy = ff_prod(w, y);
+  const FF yz = ff_prod(y, z), wx = ff_prod(w, x);
+  const FF two = {2.0f, 0.0f};
+  const FF s_ww_xx = ff_add(ww, xx), s_yy_zz = ff_add(yy, zz);
+  const FF d_ww_xx = ff_sub(ww, xx), d_yy_zz = ff_sub(yy, zz);
+  R[0][0] = ff_mul(ff_sub(s_ww_xx, s_yy_zz), inv);
+  R[1][1] = ff_mul(ff_add(d_ww_xx, d_yy_zz), inv);
+  R[2][2] = ff_mul(ff_sub(d_ww_xx, d_yy_zz), inv);
+  R[0][1] = ff_mul(ff_mul(two, ff_sub(xy, wz)), inv);
+  R[1][0] = ff_mul(ff_mul(two, ff_add(xy, wz)), inv);
+  R[0][2] = ff_mul(ff_mul(two, ff_add(xz, wy)), inv);
+  R[2][0] = ff_mul(ff_mul(two, ff_sub(xz, wy)), inv);
+  R[1][2] = ff_mul(ff_mul(two, ff_sub(yz, wx)), inv);
+  R[2][1] = ff_mul(ff_mul(two, ff_add(yz, wx)), inv);
+  return true;
+}
+
 __device__ __forceinline__ void make_frame(float4 q, const float *__restrict__ log_scale,
                                            int64_t g, Frame &f) {
-  quat_rot(q, f.rot);
+  quat_rot(q, f.rot);  // the normalised quaternion (and R for a degenerate q)
   f.s[0] = gsx_expf(log_scale[3 * g]);
   f.s[1] = gsx_expf(log_scale[3 * g + 1]);
   f.s[2] = gsx_expf(log_scale[3 * g + 2]);
+  FF R[3][3];
+  if (quat_rot_ff(q, R)) {
 #pragma unroll
-  for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < 3; ++i)
 #pragma unroll
-    for (int j = 0; j < 3; ++j) f.M[i][j] = f.s[j] * f.rot.R[i][j];
+      for (int j = 0; j < 3; ++j) {
+        f.rot.R[i][j] = R[i][j].hi;
+        f.M[i][j] = fmaf(R[i][j].hi, f.s[j], R[i][j].lo * f.s[j]);  // one rounding of R s
+      }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) f.M[i][j] = f.s[j] * f.rot.R[i][j];
+  }
 }
 
 __device__ __forceinline__ void world_cov(const Frame &f, float (&S)[3][3]) {
