@@ -99,6 +99,32 @@ __device__ __forceinline__ T block_exclusive_scan(T v, T *s_tmp, T *total) {
   return x - v + wsum;
 }
 
+// In view-major mode (view_shift > 0) a key is (view << view_shift) | local
+// tile and the range goes to the view's global tile tile_offset + local.
+__device__ __forceinline__ uint32_t range_slot(uint32_t key, uint32_t n_tiles,
+                                               const gsx_batch_view *views, int32_t n_views,
+                                               int view_shift) {
+  if (!view_shift) return key < n_tiles ? key : 0xffffffffu;
+  const uint32_t v = key >> view_shift, t = key & ((1u << view_shift) - 1u);
+  if (v >= (uint32_t)n_views) return 0xffffffffu;
+  const gsx_batch_view &vw = views[v];
+  if ((int64_t)t >= (int64_t)vw.n_tiles_w * vw.n_tiles_h) return 0xffffffffu;
+  return (uint32_t)(vw.tile_offset + t);
+}
+
+// Tile ranges written by the last tile pass (start == nullptr in every other
+// pass): a pass's output is sorted, so each tile's keys are contiguous, and a
+// key whose neighbour in its chunk's digit run holds another tile starts (or
+// ends) its tile there, while a key at either end of a run may continue the
+// tile of the neighbouring chunk: those positions go through atomicMin /
+// atomicMax on start (all ones, the largest unsigned, until set) and end (-1).
+struct RangeOut {
+  int32_t *start, *end;
+  const gsx_batch_view *views;
+  int32_t n_views, view_shift;
+  uint32_t n_tiles;
+};
+
 // Histogram of `passes` RB-bit digits (starting at bit 0) of n keys.
 template <int RB>
 __global__ void __launch_bounds__(kThreads)
@@ -127,14 +153,14 @@ __global__ void __launch_bounds__(kThreads)
 // or *n_dev when given (a count produced on the device); chunks past it exit
 // at once, and no chunk ever waits on a later one.  `status` holds RADIX
 // look-back words per chunk.
-template <int RB, int ITEMS>
-__global__ void __launch_bounds__(kThreads)
+template <int RB, int ITEMS, bool RANGES = false>
+__global__ void __launch_bounds__(kThreads, 3)  // three CTAs per SM (shared memory allows three)
     onesweep_kernel(const uint32_t *__restrict__ keys_in,
                     const uint32_t *__restrict__ vals_in, uint32_t *__restrict__ keys_out,
                     uint32_t *__restrict__ vals_out, uint32_t n_max,
                     const uint32_t *__restrict__ n_dev, int shift,
                     const uint32_t *__restrict__ pass_hist, uint32_t *status,
-                    uint32_t *chunk_counter, uint32_t *error) {
+                    uint32_t *chunk_counter, uint32_t *error, const RangeOut ro) {
   constexpr uint32_t RADIX = 1u << RB, MASK = RADIX - 1u;
   constexpr int DPT = (int)RADIX / kThreads;  // digits per thread
   constexpr int TILE = kThreads * ITEMS;
@@ -258,10 +284,30 @@ __global__ void __launch_bounds__(kThreads)
   for (uint32_t i = t; i < cnt; i += kThreads) {
     const uint32_t k = s_keys[i];
     const uint32_t d = (k >> shift) & MASK;
-    const uint32_t gpos = s_glob[d] + (i - s_cta_excl[d]);
+    const uint32_t g0 = s_cta_excl[d];
+    const uint32_t gpos = s_glob[d] + (i - g0);
     if (gpos < n) {  // always true unless a look-back wait expired
       keys_out[gpos] = k;
       vals_out[gpos] = s_vals[i];
+      if (RANGES) {
+        const uint32_t g1 = d + 1 < RADIX ? s_cta_excl[d + 1] : cnt;  // end of the digit's run
+        const bool head = i == g0, tail = i + 1 == g1;
+        const bool first = head || s_keys[i - 1] != k;
+        const bool last = tail || s_keys[i + 1] != k;
+        if (first || last) {
+          const uint32_t slot = range_slot(k, ro.n_tiles, ro.views, ro.n_views, ro.view_shift);
+          if (slot != 0xffffffffu) {
+            if (first) {
+              if (head) atomicMin(reinterpret_cast<unsigned int *>(ro.start + slot), gpos);
+              else ro.start[slot] = (int32_t)gpos;
+            }
+            if (last) {
+              if (tail) atomicMax(ro.end + slot, (int32_t)(gpos + 1));
+              else ro.end[slot] = (int32_t)(gpos + 1);
+            }
+          }
+        }
+      }
     }
   }
 }
@@ -500,19 +546,6 @@ __global__ void __launch_bounds__(kThreads)
 // start/end of every tile from the sorted tile ids: 4 consecutive keys per
 // thread (one 16-byte load; `tiles` is 16-byte aligned), their neighbours
 // from the adjacent threads' loads or, at warp edges, from memory.
-// In view-major mode (view_shift > 0) a key is (view << view_shift) | local
-// tile and the range goes to the view's global tile tile_offset + local.
-__device__ __forceinline__ uint32_t range_slot(uint32_t key, uint32_t n_tiles,
-                                               const gsx_batch_view *views, int32_t n_views,
-                                               int view_shift) {
-  if (!view_shift) return key < n_tiles ? key : 0xffffffffu;
-  const uint32_t v = key >> view_shift, t = key & ((1u << view_shift) - 1u);
-  if (v >= (uint32_t)n_views) return 0xffffffffu;
-  const gsx_batch_view &vw = views[v];
-  if ((int64_t)t >= (int64_t)vw.n_tiles_w * vw.n_tiles_h) return 0xffffffffu;
-  return (uint32_t)(vw.tile_offset + t);
-}
-
 __global__ void ranges_kernel(const uint32_t *__restrict__ tiles, const uint32_t *__restrict__ K_dev,
                               uint32_t n_tiles, int32_t *__restrict__ start,
                               int32_t *__restrict__ end, const gsx_batch_view *__restrict__ views,
@@ -624,7 +657,8 @@ inline int sort_passes(int bits) { return (bits + digit_bits(bits) - 1) / digit_
 int radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t n_max,
                const uint32_t *n_dev, int bits, uint32_t *scratch_k[2], uint32_t *scratch_v[2],
                uint32_t *final_keys, uint32_t *final_vals, uint32_t *hist, uint32_t *tickets,
-               uint32_t *status, size_t chunks_cap, uint32_t *error, cudaStream_t s) {
+               uint32_t *status, size_t chunks_cap, uint32_t *error, cudaStream_t s,
+               const RangeOut ranges = RangeOut{}) {
   const int rb = digit_bits(bits), passes = sort_passes(bits);
   if (n_max == 0 || bits == 0) return GSX_OK;
   const uint32_t radix = 1u << rb;
@@ -650,10 +684,14 @@ int radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t n_max,
     uint32_t *vo = last ? final_vals : scratch_v[p & 1];
     uint32_t *st = status + (size_t)chunks * radix * p;
     count_launches(1);
-    e = rb == 9 ? launch_pdl(onesweep_kernel<9, kItems9>, chunks, kThreads, 0, s, ki, vi, ko, vo, n_max, n_dev,
-                             rb * p, hist + radix * p, st, tickets + p, error)
-                : launch_pdl(onesweep_kernel<8, kItems>, chunks, kThreads, 0, s, ki, vi, ko, vo, n_max, n_dev,
-                             rb * p, hist + radix * p, st, tickets + p, error);
+    const bool rng = last && ranges.start;
+    const RangeOut ro = rng ? ranges : RangeOut{};
+    auto k9 = rng ? onesweep_kernel<9, kItems9, true> : onesweep_kernel<9, kItems9, false>;
+    auto k8 = rng ? onesweep_kernel<8, kItems, true> : onesweep_kernel<8, kItems, false>;
+    e = rb == 9 ? launch_pdl(k9, chunks, kThreads, 0, s, ki, vi, ko, vo, n_max, n_dev, rb * p, hist + radix * p, st,
+                             tickets + p, error, ro)
+                : launch_pdl(k8, chunks, kThreads, 0, s, ki, vi, ko, vo, n_max, n_dev, rb * p, hist + radix * p, st,
+                             tickets + p, error, ro);
     if (e != cudaSuccess) return cuda_status(e, "onesweep_kernel launch");
     ki = ko;
     vi = vo;
@@ -708,7 +746,7 @@ int look_back_selftest(void *scratch, size_t bytes, uint32_t *error_host, cudaSt
   if (e != cudaSuccess) return cuda_status(e, "look-back self-test set-up");
   count_launches(1);
   onesweep_kernel<8, kItems><<<1, kThreads, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n, nullptr, 0, hist,
-                                         status, ticket, error);
+                                                     status, ticket, error, RangeOut{});
   e = cudaGetLastError();
   uint32_t err = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(&err, error, 4, cudaMemcpyDeviceToHost, s);
@@ -808,11 +846,13 @@ int run_binning_async(int64_t n, const int32_t *rect_tl, const int32_t *rect_br,
     const int passes = sort_passes(tile_bits);
     uint32_t *tk[2] = {w.tkeys[1], w.tkeys[0]}, *tv[2] = {w.tvals[1], w.tvals[0]};
     final_keys = (passes & 1) ? w.tkeys[1] : w.tkeys[0];
+    // 4. start / end, written by the last pass
+    const RangeOut ro{start, end, views, n_views, view_shift, (uint32_t)n_tiles};
     st = radix_sort(w.tkeys[0], w.tvals[0], cap, w.k_eff, tile_bits, tk, tv, final_keys, ids_u,
-                    w.hist + 4 * 256, w.counters + 4, w.status_tile, w.tile_chunks, w.error, s);
-    if (st != GSX_OK) return st;
+                    w.hist + 4 * 256, w.counters + 4, w.status_tile, w.tile_chunks, w.error, s, ro);
+    return st;
   }
-  // 4. start / end
+  // 4. start / end of a single tile
   count_launches(1);
   e = launch_pdl(ranges_kernel, (cap + 1023) / 1024, 256, 0, s, final_keys, w.k_eff, (uint32_t)n_tiles, start,
                  end, views, n_views, view_shift);

@@ -269,8 +269,6 @@ __device__ __forceinline__ FF ff_add(FF a, FF b) {
   return {hi, lo - (hi - s)};
 }
 
-__device__ __forceinline__ FF ff_sub(FF a, FF b) { return ff_add(a, {-b.hi, -b.lo}); }
-
 __device__ __forceinline__ FF ff_mul(FF a, FF b) {
   const FF p = ff_prod(a.hi, b.hi);
   const float lo = fmaf(a.hi, b.lo, a.lo * b.hi) + p.lo;
@@ -278,29 +276,44 @@ __device__ __forceinline__ FF ff_mul(FF a, FF b) {
   return {hi, lo - (hi - p.hi)};
 }
 
-// R(q / |q|) in float-float; false (R untouched) for |q| below the 1e-12 clamp.
-__device__ __forceinline__ bool quat_rot_ff(const float4 q, FF (&R)[3][3]) {
+// R(q / |q|) in float-float, written as R (rounded) and M = R diag(s) (one
+// rounding of the float-float product) one entry at a time; false (nothing
+// written) for |q| below the 1e-12 clamp.
+__device__ __forceinline__ bool frame_ff(const float4 q, const float (&s)[3], float (&R)[3][3],
+                                         float (&M)[3][3]) {
   const float w = q.x, x = q.y, y = q.z, z = q.w;
   const FF ww = ff_prod(w, w), xx = ff_prod(x, x), yy = ff_prod(y, y), zz = ff_prod(z, z);
-  const FF n2 = ff_add(ff_add(ww, xx), ff_add(yy, zz));
+  const FF s_ww_xx = ff_add(ww, xx), s_yy_zz = ff_add(yy, zz);
+  const FF n2 = ff_add(s_ww_xx, s_yy_zz);
   if (!(n2.hi >= 1e-24f)) return false;
   const float r0 = 1.0f / n2.hi;
   const float e = fmaf(-n2.hi, r0, 1.0f) - n2.lo * r0;  // 1 - |q|^2 r0
   const FF inv = {r0, r0 * e};
-  const FF xy = ff_prod(x, y), wz = ff_prod(w, z), xz = ff_prod(x, z), wy = ff_prod(w, y);
-  const FF yz = ff_prod(y, z), wx = ff_prod(w, x);
-  const FF two = {2.0f, 0.0f};
-  const FF s_ww_xx = ff_add(ww, xx), s_yy_zz = ff_add(yy, zz);
-  const FF d_ww_xx = ff_sub(ww, xx), d_yy_zz = ff_sub(yy, zz);
-  R[0][0] = ff_mul(ff_sub(s_ww_xx, s_yy_zz), inv);
-  R[1][1] = ff_mul(ff_add(d_ww_xx, d_yy_zz), inv);
-  R[2][2] = ff_mul(ff_sub(d_ww_xx, d_yy_zz), inv);
-  R[0][1] = ff_mul(ff_mul(two, ff_sub(xy, wz)), inv);
-  R[1][0] = ff_mul(ff_mul(two, ff_add(xy, wz)), inv);
-  R[0][2] = ff_mul(ff_mul(two, ff_add(xz, wy)), inv);
-  R[2][0] = ff_mul(ff_mul(two, ff_sub(xz, wy)), inv);
-  R[1][2] = ff_mul(ff_mul(two, ff_sub(yz, wx)), inv);
-  R[2][1] = ff_mul(ff_mul(two, ff_add(yz, wx)), inv);
+  const FF inv2 = {2.0f * r0, 2.0f * (r0 * e)};  // 2 / |q|^2, exact doubling
+  auto put = [&](int i, int j, FF num, const FF &scale) {
+    const FF r = ff_mul(num, scale);
+    R[i][j] = r.hi;
+    M[i][j] = fmaf(r.hi, s[j], r.lo * s[j]);
+  };
+  const FF d_ww_xx = ff_add(ww, {-xx.hi, -xx.lo}), d_yy_zz = ff_add(yy, {-zz.hi, -zz.lo});
+  put(0, 0, ff_add(s_ww_xx, {-s_yy_zz.hi, -s_yy_zz.lo}), inv);
+  put(1, 1, ff_add(d_ww_xx, d_yy_zz), inv);
+  put(2, 2, ff_add(d_ww_xx, {-d_yy_zz.hi, -d_yy_zz.lo}), inv);
+  {
+    const FF xy = ff_prod(x, y), wz = ff_prod(w, z);
+    put(0, 1, ff_add(xy, {-wz.hi, -wz.lo}), inv2);
+    put(1, 0, ff_add(xy, wz), inv2);
+  }
+  {
+    const FF xz = ff_prod(x, z), wy = ff_prod(w, y);
+    put(0, 2, ff_add(xz, wy), inv2);
+    put(2, 0, ff_add(xz, {-wy.hi, -wy.lo}), inv2);
+  }
+  {
+    const FF yz = ff_prod(y, z), wx = ff_prod(w, x);
+    put(1, 2, ff_add(yz, {-wx.hi, -wx.lo}), inv2);
+    put(2, 1, ff_add(yz, wx), inv2);
+  }
   return true;
 }
 
@@ -310,16 +323,7 @@ __device__ __forceinline__ void make_frame(float4 q, const float *__restrict__ l
   f.s[0] = gsx_expf(log_scale[3 * g]);
   f.s[1] = gsx_expf(log_scale[3 * g + 1]);
   f.s[2] = gsx_expf(log_scale[3 * g + 2]);
-  FF R[3][3];
-  if (quat_rot_ff(q, R)) {
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        f.rot.R[i][j] = R[i][j].hi;
-        f.M[i][j] = fmaf(R[i][j].hi, f.s[j], R[i][j].lo * f.s[j]);  // one rounding of R s
-      }
-  } else {
+  if (!frame_ff(q, f.s, f.rot.R, f.M)) {
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -509,10 +513,12 @@ __global__ void __launch_bounds__(256)
   float GS[3][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};
   float ga = 0.0f;
   const float4 q = reinterpret_cast<const float4 *>(v0.qvec)[g];
-  Frame f;
-  make_frame(q, v0.log_scale, g, f);
   float Sig[3][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};
-  if (flags & GSX_GRAD_JACOBIAN) world_cov(f, Sig);
+  if (flags & GSX_GRAD_JACOBIAN) {  // the frame is made again after the view loop: fewer live registers in it
+    Frame f0;
+    make_frame(q, v0.log_scale, g, f0);
+    world_cov(f0, Sig);
+  }
   bool seen = false;
   for (int vi = 0; vi < n_views; ++vi) {
     const int64_t item = views[vi].item_offset + g;
@@ -537,6 +543,8 @@ __global__ void __launch_bounds__(256)
   for (int j = 0; j < 3; ++j) v0.g_mean[3 * g + j] = gm[j];
   float4 gq;
   float gal;
+  Frame f;
+  make_frame(q, v0.log_scale, g, f);
   finish_param_grad(f, q, v0.alpha_logit[g], g, GS, ga, flags, v0.g_log_scale, gq, gal);
   g_qvec[g] = gq;
   v0.g_alpha_logit[g] = gal;
