@@ -3,8 +3,10 @@
 // Arithmetic contract (every kernel is compiled with -fmad=false, so only the
 // fmaf() calls written here fuse; division and sqrtf are IEEE round-to-nearest,
 // denormals are kept):
-//   * gsx_expf: Cody-Waite reduction with a two-part ln2, degree-7 Taylor
-//     polynomial, 2^j through the exponent bits, +0 below -87.  The same
+//   * gsx_expf: Cody-Waite reduction with a two-part ln2 (the float split
+//     0.693145751953125 + 1.428606765330187045e-06 that the SLEEF library
+//     publishes), degree-7 Taylor polynomial, 2^j through the exponent bits,
+//     +0 below -87.  The same
 //     operation sequence is restated in the CPU oracle, so the two agree bit
 //     for bit; it replaces the CUDA expf calls of the reference
 //     (gs/src/include/kernels.h:188, shencoder.h:4).

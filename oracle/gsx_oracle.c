@@ -20,7 +20,8 @@
  *     the file is compiled with -ffp-contract=off so nothing else fuses;
  *   - division and sqrtf are IEEE correctly rounded on both sides;
  *   - exp is gsx_expf() below (Cody-Waite range reduction with a two-part
- *     ln2, degree-7 Taylor polynomial in Horner form, 2^j scaling through the
+ *     ln2 -- the float split SLEEF publishes --, degree-7 Taylor polynomial
+ *     in Horner form, 2^j scaling through the
  *     exponent bits; flush to +0 below -87).  The reference calls CUDA's
  *     expf; gsx_expf stays within 2 ulp of the correctly rounded value on the
  *     range the path uses (checked against libm in the tests).
