@@ -1654,10 +1654,17 @@ inline bool use_two_pixels_fwd(const RasterArgs &a) {
   return a.pixels_per_thread == 2 && two_pixel_tiles(a);
 }
 
+// Gaussians per shared-memory batch of the one-pixel forward.  Measured on the
+// 1080p view (256 threads per 16x16 tile): 96 -> 0.703 ms, 128 -> 0.692,
+// 160 -> 0.690, 192 -> 0.713.
+#ifndef GSX_FWD_BATCH
+#define GSX_FWD_BATCH 128
+#endif
+
 template <int C, int MAXT, bool BATCHED, bool EXTRAS, bool RGB = false>
 int launch_fwd_tt(RasterArgs a, int64_t grid, cudaStream_t s) {
   const int nthr = block_threads(a);
-  a.batch = nthr < 128 ? nthr : 128;
+  a.batch = nthr < GSX_FWD_BATCH ? nthr : GSX_FWD_BATCH;
   const size_t smem = fwd_smem<C>(a.batch, nthr);
   static size_t attr_done = 0, attr_done_p = 0;
   cudaError_t e = ensure_smem(raster_forward_kernel<C, MAXT, BATCHED, EXTRAS, RGB>, smem, attr_done);
@@ -1762,11 +1769,12 @@ int launch_bwd_tt(RasterArgs a, int64_t grid, cudaStream_t s) {
   return cuda_status(cudaGetLastError(), "raster_backward_kernel launch");
 }
 
-// Gaussians per shared-memory batch of the two-pixel backward: with 128
-// threads per 16x16 tile, 40 keeps the CTA under 56 KB of shared memory, four
-// CTAs per SM.
+// Gaussians per shared-memory batch of the two-pixel backward (a multiple of
+// 4): with 128 threads per 16x16 tile, 44 is the largest that keeps four CTAs
+// per SM (56.6 KB each; 48 needs 58.8 KB and drops to three).  Measured on
+// the 1080p view: 36 -> 1.740 ms, 40 -> 1.717, 44 -> 1.698, 48 -> 2.012.
 #ifndef GSX_BWD2_BATCH
-#define GSX_BWD2_BATCH 40
+#define GSX_BWD2_BATCH 44
 #endif
 
 template <int C>
