@@ -758,7 +758,10 @@ constexpr int kShOff = 8;
 template <int C>
 struct Grad {
   static constexpr int CC = C * C;
-  static constexpr int CSTR = CC == 16 ? 20 : (CC + 3) & ~3;
+  // per-channel stride of the SH-gradient accumulators: C*C rounded up to 4
+  // (a padded stride of 20 at C*C = 16 was measured slower: the smaller record
+  // lets the two-pixel backward hold 48-Gaussian batches at four CTAs per SM)
+  static constexpr int CSTR = (CC + 3) & ~3;
   static constexpr int NV = kShOff + 3 * CSTR;
 };
 
@@ -1770,11 +1773,12 @@ int launch_bwd_tt(RasterArgs a, int64_t grid, cudaStream_t s) {
 }
 
 // Gaussians per shared-memory batch of the two-pixel backward (a multiple of
-// 4): with 128 threads per 16x16 tile, 44 is the largest that keeps four CTAs
-// per SM (56.6 KB each; 48 needs 58.8 KB and drops to three).  Measured on
-// the 1080p view: 36 -> 1.740 ms, 40 -> 1.717, 44 -> 1.698, 48 -> 2.012.
+// 4): with 128 threads per 16x16 tile, 48 is the largest that keeps four CTAs
+// per SM (56.5 KB each; 52 needs 58.4 KB).  Measured on the 1080p view: 36 ->
+// 1.740 ms, 40 -> 1.717, 44 -> 1.698 with 20-float SH-gradient rows; 44 ->
+// 1.673 and 48 -> 1.657 with 16-float rows.
 #ifndef GSX_BWD2_BATCH
-#define GSX_BWD2_BATCH 44
+#define GSX_BWD2_BATCH 48
 #endif
 
 template <int C>
