@@ -812,9 +812,11 @@ __device__ __forceinline__ void flush_sh_group(const float *Ws, const float *Ys,
 // s_touched is set) into the global gradients: one vector reduction per chunk
 // of a record -- mean2d (v2), cov2d (v4, entries 1 and 2 both get dL/dcov01 as
 // the reference writes them), alpha, and the SH channels in 4-float chunks.
+// Each chunk is set back to zero once read, so the accumulators need no
+// clearing pass per batch (only touched records are ever written).
 template <int C>
 __device__ __forceinline__ void fold_batch_grads(const RasterArgs &a, const ViewCtx &ctx,
-                                                 const SmemLayout &L, const float *s_grad,
+                                                 const SmemLayout &L, float *s_grad,
                                                  const int *s_touched, int nk, int t, int nthr) {
   constexpr int CC = Sh<C>::CC, NV = Grad<C>::NV;
   constexpr int NCH = Grad<C>::CSTR / 4;
@@ -822,10 +824,11 @@ __device__ __forceinline__ void fold_batch_grads(const RasterArgs &a, const View
   for (int f = t; f < nk * NCHUNK; f += nthr) {
     const int j = f / NCHUNK, c = f - j * NCHUNK;
     if (!s_touched[j]) continue;
-    const float *rec = s_grad + j * NV;
+    float *rec = s_grad + j * NV;
     const int64_t id = L.ids[j];
     if (c == 0) {
       const float2 v = *reinterpret_cast<const float2 *>(rec);
+      *reinterpret_cast<float2 *>(rec) = make_float2(0.0f, 0.0f);
       if (a.vec_grads) {
         if (v.x != 0.0f || v.y != 0.0f) red_add_v2(a.g_mean2d + 2 * id, v);
       } else {
@@ -834,6 +837,7 @@ __device__ __forceinline__ void fold_batch_grads(const RasterArgs &a, const View
       }
     } else if (c == 1) {
       const float4 v = make_float4(rec[2], rec[3], rec[3], rec[4]);
+      rec[2] = rec[3] = rec[4] = 0.0f;
       if (a.vec_grads) {
         if (v.x != 0.0f || v.y != 0.0f || v.w != 0.0f) red_add_v4(a.g_cov2d + 4 * id, v);
       } else {
@@ -845,11 +849,15 @@ __device__ __forceinline__ void fold_batch_grads(const RasterArgs &a, const View
         if (v.w != 0.0f) atomicAdd(a.g_cov2d + 4 * id + 3, v.w);
       }
     } else if (c == 2) {
-      if (rec[5] != 0.0f) atomicAdd(a.g_alpha + id, rec[5]);
+      const float v = rec[5];
+      rec[5] = 0.0f;
+      if (v != 0.0f) atomicAdd(a.g_alpha + id, v);
     } else {
       const int e = c - 3, ch = e / NCH, k = 4 * (e - ch * NCH);
-      const float4 v = *reinterpret_cast<const float4 *>(rec + kShOff + ch * Grad<C>::CSTR + k);
+      float4 *src = reinterpret_cast<float4 *>(rec + kShOff + ch * Grad<C>::CSTR + k);
+      const float4 v = *src;
       if (v.x == 0.0f && v.y == 0.0f && v.z == 0.0f && v.w == 0.0f) continue;
+      *src = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       float *dst = ctx.g_sh + ((id - ctx.item_lo) * 3 + ch) * ctx.sh_stride + k;
       if (k + 4 <= CC && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
         red_add_v4(dst, v);
@@ -933,10 +941,11 @@ __global__ void __launch_bounds__(MAXT, 1024 / MAXT * 3 / 4 > 0 ? 768 / MAXT : 1
     tile_bounds(ctx, tx0, tx1, ty0, ty1);
     const float4 blk = warp_block(px, py);
 
+    // zero once; the fold puts each record it reads back to zero
+    for (int f = t; f < B * NV; f += nthr) s_grad[f] = 0.0f;
     for (int base = 0; base < n; base += B) {
       if (__syncthreads_and(done)) break;
       const int nb = min(B, n - base);
-      for (int f = t; f < nb * NV; f += nthr) s_grad[f] = 0.0f;
       for (int j = t; j < nb; j += nthr) s_touched[j] = 0;
       const int nk = load_batch<C, true>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1,
                                          s_wcount, &s_bar, PERSIST ? (nphase & 1u) : ((uint32_t)(base / B) & 1u));
@@ -1262,10 +1271,12 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 128 ? 4 : 512 / MAXT)
     tile_bounds(ctx, tx0, tx1, ty0, ty1);
     const float4 blk = warp_block2(px, py0, py1);
 
+    // the accumulators start at zero; the fold puts each record it reads
+    // back to zero, and untouched records are never written
+    for (int f = t; f < B * NV; f += nthr) s_grad[f] = 0.0f;
     for (int base = 0; base < n; base += B) {
       if (__syncthreads_and(done0 && done1)) break;
       const int nb = min(B, n - base);
-      for (int f = t; f < nb * NV; f += nthr) s_grad[f] = 0.0f;
       for (int j = t; j < nb; j += nthr) s_touched[j] = 0;
       const int nk = load_batch<C, true>(a, ctx, L, s0 + base, nb, t, nthr, tx0, tx1, ty0, ty1,
                                          s_wcount, &s_bar, PERSIST ? (nphase & 1u) : ((uint32_t)(base / B) & 1u));
