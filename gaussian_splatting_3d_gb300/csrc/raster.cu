@@ -1668,11 +1668,11 @@ inline bool use_two_pixels_fwd(const RasterArgs &a) {
   return a.pixels_per_thread == 2 && two_pixel_tiles(a);
 }
 
-// Gaussians per shared-memory batch of the one-pixel forward.  Measured on the
-// 1080p view (256 threads per 16x16 tile): 96 -> 0.703 ms, 128 -> 0.692,
-// 160 -> 0.690, 192 -> 0.713.
+// Gaussians per shared-memory batch of the one-pixel forward (44 KB at 160,
+// four CTAs per SM).  Measured on the 1080p view (256 threads per 16x16 tile):
+// 96 -> 0.703 ms, 128 -> 0.6926, 160 -> 0.6898 (three runs each), 192 -> 0.713.
 #ifndef GSX_FWD_BATCH
-#define GSX_FWD_BATCH 128
+#define GSX_FWD_BATCH 160
 #endif
 
 template <int C, int MAXT, bool BATCHED, bool EXTRAS, bool RGB = false>
