@@ -1300,10 +1300,10 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 128 ? 4 : 512 / MAXT)
         if (!(done0 && done1)) {
           // both pixels' decision paths side by side, without branches: the
           // radial of gs/src/include/kernels.h:172-187 (one det per Gaussian,
-          // IEEE division), then the exact exponential where it can decide
-          // The two pixels share x (same column); every other step runs as
-          // a paired float2 operation, each half rounded as its scalar form
-          // (-(y*z) == y*(-z) and a - b == a + (-b) exactly).
+          // IEEE division), then the exact exponential.  The two pixels share
+          // x (same column); every other step runs as a paired float2
+          // operation, each half rounded as its scalar form (-(y*z) ==
+          // y*(-z) and a - b == a + (-b) exactly).
           const float2 h = L.box[i];
           const float x = px - m.x;
           const float2 y = __fadd2_rn(f2(py0, py1), f2(-m.y, -m.y));
